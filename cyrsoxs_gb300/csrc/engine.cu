@@ -1,0 +1,738 @@
+// GB300 scattering engine: host orchestration and the C ABI (include/cyrsoxs.h).
+//
+// One request = one morphology with its energies, k vectors and E angles.
+// The path per energy (src/cudaMain.cu:586-971 restated for one GPU):
+//
+//   LAB frame (default): the polarization is linear in E (p = Nt E / 4pi,
+//   include/uniaxial.h:75, :106-151), and the window, the FFT, the DC
+//   replacement and the shift are linear too, so the spectrum of every E
+//   angle is  P(angle) = sum_b E_b(angle) FFT(Nt e_b).  The engine transforms
+//   the 5 (k along z) or 6 distinct entries of the symmetric tensor Nt once
+//   per energy and forms each angle's intensity from them in the Ewald
+//   kernel, instead of 3 FFTs per angle.
+//   MATERIAL frame: p = R^T Nt R x depends on the angle non-linearly; the
+//   engine runs the reference's per-angle schedule (3 volumes per angle).
+//
+//   k_build -> k_fft_pass<x,y,z> -> k_dc -> per k: k_ewald_angles ->
+//   k_rotate_average -> k_fill + k_warp (detector) -> projection[e][k]
+//
+// All per-request constants (optical constants of every energy, angle
+// coefficients, warp coefficients, q-grid and window tables) are computed on
+// the host in double and uploaded once, before any kernel of the request.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cyrsoxs.h"
+#include "geometry.h"
+#include "kernels.cuh"
+
+namespace cyr {
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return code;
+}
+
+#define CYR_CUDA(call)                                                                               \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess)                                                                           \
+      return fail(e_ == cudaErrorMemoryAllocation ? CYR_ERR_MEMORY : CYR_ERR_CUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                                \
+  } while (0)
+
+#define CYR_TRY(expr)         \
+  do {                        \
+    int rc_ = (expr);         \
+    if (rc_ != CYR_OK) return rc_; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// FFT plans
+// ---------------------------------------------------------------------------
+bool factorize(uint32_t n, std::vector<uint32_t> &radix) {
+  radix.clear();
+  uint32_t r = n;
+  while (r % 8 == 0) radix.push_back(8), r /= 8;
+  while (r % 4 == 0) radix.push_back(4), r /= 4;
+  while (r % 2 == 0) radix.push_back(2), r /= 2;
+  for (uint32_t p : {3u, 5u, 7u})
+    while (r % p == 0) radix.push_back(p), r /= p;
+  return r == 1 && radix.size() <= 16;
+}
+
+constexpr size_t kFftSmemBudget = 200 * 1024;
+
+uint32_t fft_lines_per_block(uint32_t n) {
+  uint32_t tx = 16;
+  while (tx > 1 && size_t(2) * n * (tx + 1) * sizeof(float2) > kFftSmemBudget) tx /= 2;
+  return tx;
+}
+
+// ---------------------------------------------------------------------------
+// Per-device context: cached twiddle tables and grow-only scratch.
+// ---------------------------------------------------------------------------
+struct DeviceBuffer {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need) {
+    if (need <= bytes) return CYR_OK;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    if (need == 0) return CYR_OK;
+    CYR_CUDA(cudaMalloc(&ptr, need));
+    bytes = need;
+    return CYR_OK;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(ptr);
+  }
+};
+
+struct DeviceContext {
+  int device = -1;
+  std::mutex mu;
+  bool attrs_done = false;
+  std::map<uint32_t, float2 *> twiddles;
+  DeviceBuffer spec, images, avg, params, dc, vox_in, out_in;
+  cudaEvent_t last_use = nullptr;  // completion of the last request that used the scratch
+};
+
+std::mutex g_ctx_mu;
+std::map<int, std::unique_ptr<DeviceContext>> g_ctx;
+
+int get_context(DeviceContext **out) {
+  int dev = 0;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count < 1) {
+    cudaGetLastError();
+    return fail(CYR_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  CYR_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  auto &slot = g_ctx[dev];
+  if (!slot) {
+    slot.reset(new DeviceContext);
+    slot->device = dev;
+  }
+  *out = slot.get();
+  return CYR_OK;
+}
+
+int setup_attrs(DeviceContext &ctx) {
+  if (ctx.attrs_done) return CYR_OK;
+  const int smem = int(kFftSmemBudget);
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_CUDA(cudaEventCreateWithFlags(&ctx.last_use, cudaEventDisableTiming));
+  ctx.attrs_done = true;
+  return CYR_OK;
+}
+
+int get_twiddles(DeviceContext &ctx, uint32_t n, const float2 **tw) {
+  auto it = ctx.twiddles.find(n);
+  if (it != ctx.twiddles.end()) {
+    *tw = it->second;
+    return CYR_OK;
+  }
+  std::vector<float2> h(n);
+  for (uint32_t m = 0; m < n; ++m) {
+    const double a = -2.0 * kPi * double(m) / double(n);  // W_n^m = exp(-2 pi i m / n), in double
+    h[m] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+  }
+  float2 *d = nullptr;
+  CYR_CUDA(cudaMalloc(&d, sizeof(float2) * n));
+  CYR_CUDA(cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+  ctx.twiddles[n] = d;
+  *tw = d;
+  return CYR_OK;
+}
+
+int make_axis(DeviceContext &ctx, uint32_t n, FftAxis &ax) {
+  std::vector<uint32_t> r;
+  if (!factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u has a prime factor above 7", n);
+  ax.n = n;
+  ax.nstages = uint32_t(r.size());
+  for (size_t i = 0; i < r.size(); ++i) ax.radix[i] = r[i];
+  return get_twiddles(ctx, n, &ax.tw);
+}
+
+// In-place forward 3D FFT of `count` volumes.
+int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st) {
+  const size_t nvox = size_t(nx) * ny * nz;
+  const uint32_t dims[3] = {nx, ny, nz};
+  for (int axis = 0; axis < 3; ++axis) {
+    const uint32_t n = dims[axis];
+    if (n == 1) continue;
+    FftPassParams p{};
+    p.data = data;
+    p.nx = nx, p.ny = ny, p.nz = nz;
+    p.nvox = nvox;
+    CYR_TRY(make_axis(ctx, n, p.ax));
+    p.tx = fft_lines_per_block(n);
+    const size_t smem = size_t(2) * n * (p.tx + 1) * sizeof(float2);
+    if (smem > kFftSmemBudget) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u too large for one block", n);
+    uint32_t tiles;
+    if (axis == 0) {
+      tiles = (ny * nz + p.tx - 1) / p.tx;
+    } else {
+      const uint32_t nxt = (nx + p.tx - 1) / p.tx;
+      tiles = nxt * (axis == 1 ? nz : ny);
+    }
+    const dim3 grid(tiles, count);
+    if (axis == 0) k_fft_pass<0><<<grid, 256, smem, st>>>(p);
+    if (axis == 1) k_fft_pass<1><<<grid, 256, smem, st>>>(p);
+    if (axis == 2) k_fft_pass<2><<<grid, 256, smem, st>>>(p);
+    CYR_CUDA(cudaGetLastError());
+  }
+  return CYR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Request planning
+// ---------------------------------------------------------------------------
+struct Plan {
+  uint32_t nx, ny, nz, nmat, ne, nk, nang;
+  size_t nvox, npix;
+  bool material_frame, hanning, twod;
+  uint32_t nbasis, nvol;           // LAB: 2 or 3 bases; MATERIAL: 1 basis, 3 volumes
+  std::vector<KFrame> frames;
+  Mat3f detector;
+  std::vector<float> start_inc;    // start, inc
+  // host parameter arena, uploaded once
+  std::vector<unsigned char> arena;
+  size_t off_mc = 0, off_coef = 0, off_warp = 0, off_qx = 0, off_qy = 0, off_qz = 0, off_hx = 0, off_hy = 0, off_hz = 0;
+  std::vector<WarpCoef> detector_warp;  // per k
+  std::vector<float> evec;              // [k][angle][3] E = R x
+  std::vector<Mat3f> rmats;             // [k][angle] (MATERIAL frame)
+  std::vector<float> eangles;           // [k][angle]
+  float start, inc;
+};
+
+template <class T>
+size_t arena_put(std::vector<unsigned char> &a, const T *src, size_t count) {
+  size_t off = (a.size() + 255) & ~size_t(255);
+  a.resize(off + sizeof(T) * count);
+  if (count) std::memcpy(a.data() + off, src, sizeof(T) * count);
+  return off;
+}
+
+int validate(const cyr_options *o) {
+  if (!o) return fail(CYR_ERR_ARGUMENT, "options pointer is null");
+  if (o->nx < 2 || o->ny < 2 || o->nz < 1) return fail(CYR_ERR_ARGUMENT, "dimensions must be nx, ny >= 2, nz >= 1");
+  if (o->num_material < 1 || o->num_material > uint32_t(kMaxMaterials))
+    return fail(CYR_ERR_ARGUMENT, "num_material must be in [1, %d]", kMaxMaterials);
+  if (o->num_energies < 1 || !o->energies) return fail(CYR_ERR_ARGUMENT, "no energies");
+  if (!(o->phys_size > 0)) return fail(CYR_ERR_ARGUMENT, "phys_size must be positive");
+  if (o->case_type > 2) return fail(CYR_ERR_ARGUMENT, "case_type must be 0, 1 or 2");
+  if (o->case_type != 0 && (o->num_k < 1 || !o->k_vectors)) return fail(CYR_ERR_ARGUMENT, "k vectors missing");
+  if (o->morphology_type > 1 || o->ewald_interpolation > 1 || o->windowing > 1 || o->scatter_approach > 1 ||
+      o->algorithm > 1 || o->reference_frame > 1)
+    return fail(CYR_ERR_ARGUMENT, "enumerated option out of range");
+  if (o->start_angle > o->end_angle) return fail(CYR_ERR_ARGUMENT, "start angle greater than end angle");
+  if (!near_equal(o->start_angle, o->end_angle) && near_equal(o->increment_angle, 0.f))
+    return fail(CYR_ERR_ARGUMENT, "increment angle is 0");
+  for (uint32_t e = 0; e < o->num_energies; ++e)
+    if (!(o->energies[e] > 0)) return fail(CYR_ERR_ARGUMENT, "energies must be positive");
+  std::vector<uint32_t> r;
+  const uint32_t d[3] = {o->nx, o->ny, o->nz};
+  for (uint32_t n : d)
+    if (n > 1 && !factorize(n, r))
+      return fail(CYR_ERR_UNSUPPORTED, "dimension %u has a prime factor above 7 (supported: 2^a 3^b 5^c 7^d)", n);
+  for (uint32_t n : d)
+    if (n > 1 && size_t(2) * n * 2 * sizeof(float2) > kFftSmemBudget)
+      return fail(CYR_ERR_UNSUPPORTED, "dimension %u exceeds the single-block FFT limit", n);
+  return CYR_OK;
+}
+
+int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
+  CYR_TRY(validate(o));
+  if (!optical) return fail(CYR_ERR_ARGUMENT, "optical constants pointer is null");
+  pl.nx = o->nx, pl.ny = o->ny, pl.nz = o->nz, pl.nmat = o->num_material, pl.ne = o->num_energies;
+  pl.nvox = size_t(pl.nx) * pl.ny * pl.nz;
+  pl.npix = size_t(pl.nx) * pl.ny;
+  pl.twod = pl.nz == 1;
+  pl.material_frame = o->reference_frame == 0;
+  pl.hanning = o->algorithm == 0 && o->windowing == 1;
+  // E-angle schedule (InputData::setEAngles, src/cudaMain.cu:393-394)
+  pl.start = o->start_angle;
+  pl.inc = near_equal(o->start_angle, o->end_angle) ? 1.0f : o->increment_angle;
+  const float nang_f = std::round((o->end_angle - o->start_angle) / pl.inc + 1);
+  if (!(nang_f >= 1) || nang_f > float(kMaxAngles)) return fail(CYR_ERR_ARGUMENT, "angle count out of range");
+  pl.nang = uint32_t(nang_f);
+  // k vectors and frames (src/RotationMatrix.cpp:30-51)
+  std::vector<Vec3f> ks;
+  if (o->case_type == 0 && (o->num_k == 0 || !o->k_vectors)) {
+    ks.push_back({0.f, 0.f, 1.f});
+  } else {
+    for (uint32_t i = 0; i < o->num_k; ++i) ks.push_back({o->k_vectors[3 * i], o->k_vectors[3 * i + 1], o->k_vectors[3 * i + 2]});
+  }
+  pl.nk = uint32_t(ks.size());
+  for (const Vec3f &k : ks) pl.frames.push_back(make_kframe(k));
+  const Vec3f det = o->case_type == 2 ? Vec3f{o->detector[0], o->detector[1], o->detector[2]} : Vec3f{0.f, 0.f, 1.f};
+  pl.detector = rotation_between({0.f, 0.f, 1.f}, det);
+  // per (k, angle): E angle, rotation, E vector
+  bool any_ez = false;
+  pl.evec.resize(size_t(pl.nk) * pl.nang * 3);
+  pl.rmats.resize(size_t(pl.nk) * pl.nang);
+  pl.eangles.resize(size_t(pl.nk) * pl.nang);
+  for (uint32_t k = 0; k < pl.nk; ++k)
+    for (uint32_t a = 0; a < pl.nang; ++a) {
+      const float ang = e_angle(pl.frames[k], pl.start, pl.inc, a);
+      const Mat3f R = e_rotation(pl.frames[k], ang);
+      const size_t ka = size_t(k) * pl.nang + a;
+      pl.eangles[ka] = ang;
+      pl.rmats[ka] = R;
+      pl.evec[ka * 3 + 0] = R(0, 0);
+      pl.evec[ka * 3 + 1] = R(1, 0);
+      pl.evec[ka * 3 + 2] = R(2, 0);
+      if (R(2, 0) != 0.f) any_ez = true;
+    }
+  if (pl.material_frame) {
+    pl.nbasis = 1;
+    pl.nvol = 3;
+  } else {
+    pl.nbasis = any_ez ? 3 : 2;
+    pl.nvol = any_ez ? 6 : 5;
+  }
+  // material constants per energy, in double, scaled by 1/4pi (uniaxial.h:155-162)
+  std::vector<MaterialConsts> mcs(pl.ne);
+  const double s = 1.0 / (4.0 * kPi);
+  for (uint32_t e = 0; e < pl.ne; ++e) {
+    MaterialConsts &mc = mcs[e];
+    std::memset(&mc, 0, sizeof mc);
+    for (uint32_t m = 0; m < pl.nmat; ++m) {
+      const float *op = optical + (size_t(e) * pl.nmat + m) * 4;
+      const std::complex<double> dpar(-double(op[0]), double(op[1]));  // n_par - 1
+      const std::complex<double> dper(-double(op[2]), double(op[3]));  // n_perp - 1
+      const std::complex<double> A = dpar * (dpar + 2.0);              // n^2 - 1 = (n-1)(n+1)
+      const std::complex<double> B = dper * (dper + 2.0);
+      const std::complex<double> dm = (dpar + 2.0 * dper) / 3.0;       // mean n - 1
+      const std::complex<double> C = dm * (dm + 2.0);
+      const std::complex<double> D = A - B;
+      mc.A[m] = make_float2(float(A.real() * s), float(A.imag() * s));
+      mc.B[m] = make_float2(float(B.real() * s), float(B.imag() * s));
+      mc.C[m] = make_float2(float(C.real() * s), float(C.imag() * s));
+      mc.D[m] = make_float2(float(D.real() * s), float(D.imag() * s));
+    }
+  }
+  pl.arena.clear();
+  pl.off_mc = arena_put(pl.arena, mcs.data(), mcs.size());
+  // angle coefficients [k][angle][nbasis]
+  std::vector<float> coef(size_t(pl.nk) * pl.nang * pl.nbasis);
+  for (size_t ka = 0; ka < size_t(pl.nk) * pl.nang; ++ka)
+    for (uint32_t b = 0; b < pl.nbasis; ++b) coef[ka * pl.nbasis + b] = pl.material_frame ? 1.f : pl.evec[ka * 3 + b];
+  pl.off_coef = arena_put(pl.arena, coef.data(), coef.size());
+  // per-angle image rotation coefficients [k][angle] (src/cudaMain.cu:848-855)
+  std::vector<WarpCoef> wc(size_t(pl.nk) * pl.nang);
+  for (size_t ka = 0; ka < wc.size(); ++ka) {
+    double c[2][3];
+    rotation_coeffs(pl.eangles[ka], pl.nx, pl.ny, c);
+    const WarpInverse w = warp_inverse(c);
+    wc[ka] = WarpCoef{w.a00, w.a01, w.a02, w.a10, w.a11, w.a12};
+  }
+  pl.off_warp = arena_put(pl.arena, wc.data(), wc.size());
+  // detector warps per k (src/cudaMain.cu:916-940)
+  pl.detector_warp.resize(pl.nk);
+  for (uint32_t k = 0; k < pl.nk; ++k) {
+    double c[2][3];
+    detector_coeffs(pl.detector, pl.frames[k].rk, pl.nx, pl.ny, c);
+    const WarpInverse w = warp_inverse(c);
+    pl.detector_warp[k] = WarpCoef{w.a00, w.a01, w.a02, w.a10, w.a11, w.a12};
+  }
+  // q-grid tables (include/uniaxial.h:645-650, :697-702): q_j = float(-pi/L + j * float(dq))
+  const double L = double(o->phys_size);
+  auto qtab = [&](uint32_t n) {
+    std::vector<float> q(n, 0.f);
+    if (n < 2) return q;
+    const float dq = static_cast<float>((2 * kPi / L) / ((n - 1) * 1.0));
+    for (uint32_t j = 0; j < n; ++j) q[j] = static_cast<float>((-kPi / L) + double(float(j) * dq));
+    return q;
+  };
+  const std::vector<float> qx = qtab(pl.nx), qy = qtab(pl.ny), qz = qtab(pl.nz);
+  pl.off_qx = arena_put(pl.arena, qx.data(), qx.size());
+  pl.off_qy = arena_put(pl.arena, qy.data(), qy.size());
+  pl.off_qz = arena_put(pl.arena, qz.data(), qz.size());
+  // Hanning tables (src/cudaMain.cu:276-295), double cos rounded to float
+  auto hann = [&](uint32_t n, bool unit) {
+    std::vector<float> w(n);
+    for (uint32_t j = 0; j < n; ++j) w[j] = unit ? 1.f : static_cast<float>(0.5 * (1 - std::cos(2 * kPi * j / n)));
+    return w;
+  };
+  const std::vector<float> hx = hann(pl.nx, false), hy = hann(pl.ny, false), hz = hann(pl.nz, pl.twod);
+  pl.off_hx = arena_put(pl.arena, hx.data(), hx.size());
+  pl.off_hy = arena_put(pl.arena, hy.data(), hy.size());
+  pl.off_hz = arena_put(pl.arena, hz.data(), hz.size());
+  pl.arena.resize((pl.arena.size() + 255) & ~size_t(255));
+  return CYR_OK;
+}
+
+size_t request_bytes(const Plan &pl) {
+  return pl.nvol * pl.nvox * sizeof(float2) + size_t(pl.nang) * pl.npix * sizeof(float) + pl.npix * sizeof(float) +
+         pl.arena.size() + 64 * sizeof(float2);
+}
+
+// Ewald-kernel parameters shared by every (energy, k).
+EwaldParams ewald_params(const Plan &pl, const cyr_options *o, const unsigned char *dparams, const float2 *spec,
+                         const float2 *dc, float *images) {
+  EwaldParams p{};
+  p.spec = spec;
+  p.dc = dc;
+  p.nx = pl.nx, p.ny = pl.ny, p.nz = pl.nz;
+  p.nvox = pl.nvox;
+  p.nbasis = pl.nbasis;
+  if (pl.material_frame) {
+    for (int c = 0; c < 3; ++c) p.vol[c][0] = c;
+  } else {
+    // symmetric tensor entry (c, b) -> output volume; volumes hold xx xy xz yy yz [zz]
+    const uint32_t sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    for (int c = 0; c < 3; ++c)
+      for (uint32_t b = 0; b < pl.nbasis; ++b) p.vol[c][b] = sym[c][b];
+  }
+  p.start = -static_cast<float>(kPi / o->phys_size);
+  p.dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nx - 1) * 1.0));
+  p.dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.ny - 1) * 1.0));
+  p.dz = pl.twod ? 0.f : static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nz - 1) * 1.0));
+  p.qx = reinterpret_cast<const float *>(dparams + pl.off_qx);
+  p.qy = reinterpret_cast<const float *>(dparams + pl.off_qy);
+  p.qz = reinterpret_cast<const float *>(dparams + pl.off_qz);
+  p.interp = o->ewald_interpolation;
+  p.twod = pl.twod ? 1u : 0u;
+  p.images = images;
+  return p;
+}
+
+int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, const float4 *d_vox, float *d_out,
+                cudaStream_t st) {
+  Plan pl;
+  CYR_TRY(make_plan(o, optical, pl));
+  CYR_TRY(setup_attrs(ctx));
+  // scratch (grow-only); wait for the previous user of the scratch
+  CYR_CUDA(cudaStreamWaitEvent(st, ctx.last_use, 0));
+  CYR_TRY(ctx.spec.ensure(pl.nvol * pl.nvox * sizeof(float2)));
+  CYR_TRY(ctx.images.ensure(size_t(pl.nang) * pl.npix * sizeof(float)));
+  CYR_TRY(ctx.avg.ensure(pl.npix * sizeof(float)));
+  CYR_TRY(ctx.dc.ensure(8 * sizeof(float2)));
+  CYR_TRY(ctx.params.ensure(pl.arena.size()));
+  CYR_CUDA(cudaMemcpyAsync(ctx.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
+  const unsigned char *dp = ctx.params.as<unsigned char>();
+  float2 *spec = ctx.spec.as<float2>();
+  float2 *dc = ctx.dc.as<float2>();
+  float *images = ctx.images.as<float>();
+  float *avg = ctx.avg.as<float>();
+  const MaterialConsts *dmc = reinterpret_cast<const MaterialConsts *>(dp + pl.off_mc);
+
+  BuildParams bp{};
+  bp.vox = d_vox;
+  bp.nx = pl.nx, bp.ny = pl.ny, bp.nz = pl.nz, bp.nmat = pl.nmat;
+  bp.nvox = pl.nvox;
+  bp.morphology = o->morphology_type;
+  bp.out = spec;
+  if (pl.hanning) {
+    bp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
+    bp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
+    bp.hann_z = reinterpret_cast<const float *>(dp + pl.off_hz);
+  }
+  int sms = 0;
+  CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  const uint32_t build_blocks = uint32_t(std::min<size_t>((pl.nvox + 255) / 256, size_t(sms) * 8));
+  EwaldParams ep = ewald_params(pl, o, dp, spec, dc, images);
+  const unsigned pix_blocks = unsigned((pl.npix + 255) / 256);
+  const int W = int(pl.ny), H = int(pl.nx);  // the reference hands NPP width = Ny, height = Nx
+  const WarpCoef *dwarp = reinterpret_cast<const WarpCoef *>(dp + pl.off_warp);
+  const float *dcoef = reinterpret_cast<const float *>(dp + pl.off_coef);
+
+  for (uint32_t e = 0; e < pl.ne; ++e) {
+    const MaterialConsts *mce = dmc + e;
+    const float energy = o->energies[e];
+    const float wavelength = static_cast<float>(1239.84197 / energy);  // src/cudaMain.cu:607-608
+    const float kmag = static_cast<float>(2 * kPi / wavelength);
+    ep.kmag = kmag;
+    if (!pl.material_frame) {
+      // tensor entries once per energy: xx xy xz yy yz [zz]
+      bp.mode = 0;
+      bp.nvol = pl.nvol;
+      for (uint32_t v = 0; v < 6; ++v) bp.entry[v] = v;
+      if (o->morphology_type == 0)
+        k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
+      else
+        k_build<1><<<build_blocks, 256, 0, st>>>(bp, mce);
+      CYR_CUDA(cudaGetLastError());
+      CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, pl.nvol, st));
+      k_dc<<<1, 32, 0, st>>>(spec, pl.nvol, pl.nvox, pl.nx, pl.ny, pl.nz, dc);
+      CYR_CUDA(cudaGetLastError());
+    }
+    for (uint32_t k = 0; k < pl.nk; ++k) {
+      const KFrame &f = pl.frames[k];
+      ep.kvx = f.k.x, ep.kvy = f.k.y, ep.kvz = f.k.z;
+      ep.kx = kmag * f.k.x, ep.ky = kmag * f.k.y, ep.kz = kmag * f.k.z;
+      if (!pl.material_frame) {
+        ep.nangles = pl.nang;
+        ep.coef = dcoef + size_t(k) * pl.nang * pl.nbasis;
+        ep.images = images;
+        k_ewald_angles<<<pix_blocks, 256, 0, st>>>(ep);
+        CYR_CUDA(cudaGetLastError());
+      } else {
+        // per-angle schedule: p(angle) -> FFT -> DC -> Ewald into image slot a
+        for (uint32_t a = 0; a < pl.nang; ++a) {
+          const size_t ka = size_t(k) * pl.nang + a;
+          bp.mode = 1;
+          bp.nvol = 3;
+          bp.material_frame = 1;
+          for (int c = 0; c < 3; ++c) bp.E[c] = pl.evec[ka * 3 + c];
+          std::memcpy(bp.Rm, pl.rmats[ka].m, sizeof bp.Rm);
+          if (o->morphology_type == 0)
+            k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
+          else
+            k_build<1><<<build_blocks, 256, 0, st>>>(bp, mce);
+          CYR_CUDA(cudaGetLastError());
+          CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, 3, st));
+          k_dc<<<1, 32, 0, st>>>(spec, 3, pl.nvox, pl.nx, pl.ny, pl.nz, dc);
+          ep.nangles = 1;
+          ep.coef = dcoef + ka;  // nbasis == 1, coefficient 1
+          ep.images = images + size_t(a) * pl.npix;
+          k_ewald_angles<<<pix_blocks, 256, 0, st>>>(ep);
+          CYR_CUDA(cudaGetLastError());
+        }
+      }
+      RotateParams rp{};
+      rp.images = images;
+      rp.coef = dwarp + size_t(k) * pl.nang;
+      rp.W = W, rp.H = H;
+      rp.nangles = pl.nang;
+      rp.rot_mask = o->rot_mask;
+      rp.avg = avg;
+      k_rotate_average<<<pix_blocks, 256, 0, st>>>(rp);
+      CYR_CUDA(cudaGetLastError());
+      float *dst = d_out + (size_t(e) * pl.nk + k) * pl.npix;
+      k_fill<<<pix_blocks, 256, 0, st>>>(dst, pl.npix, o->rot_mask ? 0.f : std::numeric_limits<float>::quiet_NaN());
+      k_warp<<<pix_blocks, 256, 0, st>>>(avg, dst, W, H, pl.detector_warp[k]);
+      CYR_CUDA(cudaGetLastError());
+    }
+  }
+  CYR_CUDA(cudaEventRecord(ctx.last_use, st));
+  return CYR_OK;
+}
+
+}  // namespace
+}  // namespace cyr
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using namespace cyr;
+
+extern "C" {
+
+const char *cyr_last_error(void) { return g_error.c_str(); }
+
+const char *cyr_version(void) { return "cyrsoxs-gb300 0.1 (sm_103a)"; }
+
+int cyr_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return n;
+}
+
+int cyr_required_device_bytes(const cyr_options *opt, size_t *bytes) {
+  if (!bytes) return fail(CYR_ERR_ARGUMENT, "bytes pointer is null");
+  CYR_TRY(validate(opt));
+  std::vector<float> dummy(size_t(opt->num_energies) * opt->num_material * 4, 0.f);
+  Plan pl;
+  CYR_TRY(make_plan(opt, dummy.data(), pl));
+  *bytes = request_bytes(pl);
+  return CYR_OK;
+}
+
+int cyr_release_scratch(void) {
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CYR_CUDA(cudaDeviceSynchronize());
+  ctx->spec.release();
+  ctx->images.release();
+  ctx->avg.release();
+  ctx->params.release();
+  ctx->dc.release();
+  ctx->vox_in.release();
+  ctx->out_in.release();
+  return CYR_OK;
+}
+
+int cyr_simulate_device(const cyr_options *opt, const float *optical, const void *d_voxels, float *d_projection,
+                        void *stream) {
+  if (!d_voxels || !d_projection) return fail(CYR_ERR_ARGUMENT, "device pointer is null");
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return run_request(*ctx, opt, optical, static_cast<const float4 *>(d_voxels), d_projection,
+                     static_cast<cudaStream_t>(stream));
+}
+
+static int cuda_main_impl(const cyr_options *opt, const float *optical, const float *voxels, float *projection,
+                          bool streams_variant) {
+  if (!voxels || !projection) return fail(CYR_ERR_ARGUMENT, "host pointer is null");
+  CYR_TRY(validate(opt));
+  cyr_options o = *opt;
+  if (streams_variant) o.algorithm = 1;
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  const size_t nvox = size_t(o.nx) * o.ny * o.nz;
+  const size_t vox_bytes = nvox * o.num_material * sizeof(float4);
+  const uint32_t nk = (o.case_type == 0 && (o.num_k == 0 || !o.k_vectors)) ? 1u : o.num_k;
+  const size_t out_bytes = size_t(o.num_energies) * nk * o.nx * o.ny * sizeof(float);
+  CYR_TRY(ctx->vox_in.ensure(vox_bytes));
+  CYR_TRY(ctx->out_in.ensure(out_bytes));
+  cudaStream_t st = nullptr;
+  CYR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  int rc = CYR_OK;
+  do {
+    if (cudaMemcpyAsync(ctx->vox_in.ptr, voxels, vox_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "voxel upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    rc = run_request(*ctx, &o, optical, ctx->vox_in.as<float4>(), ctx->out_in.as<float>(), st);
+    if (rc != CYR_OK) break;
+    if (cudaMemcpyAsync(projection, ctx->out_in.ptr, out_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "projection download failed: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(CYR_ERR_CUDA, "simulation failed: %s", cudaGetErrorString(e));
+  } while (false);
+  cudaStreamDestroy(st);
+  return rc;
+}
+
+int cyr_cuda_main(const cyr_options *opt, const float *optical, const float *voxels, float *projection) {
+  return cuda_main_impl(opt, optical, voxels, projection, false);
+}
+
+int cyr_cuda_main_streams(const cyr_options *opt, const float *optical, const float *voxels, float *projection) {
+  return cuda_main_impl(opt, optical, voxels, projection, true);
+}
+
+int cyr_compute_polarization(const cyr_options *opt, const float *optical, const float *voxels, float eangle,
+                             uint32_t energy_id, float *px, float *py, float *pz) {
+  if (!voxels || !px || !py || !pz) return fail(CYR_ERR_ARGUMENT, "host pointer is null");
+  Plan pl;
+  CYR_TRY(make_plan(opt, optical, pl));
+  if (opt->case_type != 0) return fail(CYR_ERR_UNSUPPORTED, "only implemented for case type 0 (as the reference)");
+  if (energy_id >= pl.ne) return fail(CYR_ERR_ARGUMENT, "energy id out of range");
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CYR_TRY(setup_attrs(*ctx));
+  const size_t vox_bytes = pl.nvox * pl.nmat * sizeof(float4);
+  CYR_TRY(ctx->vox_in.ensure(vox_bytes));
+  CYR_TRY(ctx->spec.ensure(3 * pl.nvox * sizeof(float2)));
+  CYR_TRY(ctx->params.ensure(pl.arena.size()));
+  cudaStream_t st = nullptr;
+  CYR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  int rc = CYR_OK;
+  do {
+    cudaStreamWaitEvent(st, ctx->last_use, 0);
+    cudaMemcpyAsync(ctx->params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(ctx->vox_in.ptr, voxels, vox_bytes, cudaMemcpyHostToDevice, st);
+    const unsigned char *dp = ctx->params.as<unsigned char>();
+    BuildParams bp{};
+    bp.vox = ctx->vox_in.as<float4>();
+    bp.nx = pl.nx, bp.ny = pl.ny, bp.nz = pl.nz, bp.nmat = pl.nmat;
+    bp.nvox = pl.nvox;
+    bp.morphology = opt->morphology_type;
+    bp.mode = 1;
+    bp.nvol = 3;
+    bp.out = ctx->spec.as<float2>();
+    bp.material_frame = pl.material_frame ? 1u : 0u;
+    // the debug path rotates E by EAngle radians about k (src/cudaMain.cu:1716-1721)
+    const Mat3f R = e_rotation(pl.frames[0], eangle);
+    for (int c = 0; c < 3; ++c) bp.E[c] = R(c, 0);
+    std::memcpy(bp.Rm, R.m, sizeof bp.Rm);
+    if (opt->windowing == 1) {  // the debug path windows whatever the algorithm (src/cudaMain.cu:1722-1725)
+      bp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
+      bp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
+      bp.hann_z = reinterpret_cast<const float *>(dp + pl.off_hz);
+    }
+    const MaterialConsts *mce = reinterpret_cast<const MaterialConsts *>(dp + pl.off_mc) + energy_id;
+    const uint32_t blocks = uint32_t(std::min<size_t>((pl.nvox + 255) / 256, 65535));
+    if (opt->morphology_type == 0)
+      k_build<0><<<blocks, 256, 0, st>>>(bp, mce);
+    else
+      k_build<1><<<blocks, 256, 0, st>>>(bp, mce);
+    if (cudaGetLastError() != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "polarization kernel launch failed");
+      break;
+    }
+    const size_t cb = pl.nvox * sizeof(float2);
+    cudaMemcpyAsync(px, ctx->spec.as<float2>(), cb, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(py, ctx->spec.as<float2>() + pl.nvox, cb, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(pz, ctx->spec.as<float2>() + 2 * pl.nvox, cb, cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(ctx->last_use, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(CYR_ERR_CUDA, "polarization failed: %s", cudaGetErrorString(e));
+  } while (false);
+  cudaStreamDestroy(st);
+  return rc;
+}
+
+int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, void *stream) {
+  if (!d_data || nx < 1 || ny < 1 || nz < 1 || count < 1) return fail(CYR_ERR_ARGUMENT, "bad FFT arguments");
+  std::vector<uint32_t> r;
+  for (uint32_t n : {nx, ny, nz})
+    if (n > 1 && !factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u has a prime factor above 7", n);
+  if (count > 65535) return fail(CYR_ERR_ARGUMENT, "too many volumes in one call");
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CYR_TRY(setup_attrs(*ctx));
+  return fft3d(*ctx, static_cast<float2 *>(d_data), nx, ny, nz, count, static_cast<cudaStream_t>(stream));
+}
+
+int cyr_warp_affine_device(const float *d_src, float *d_dst, int width, int height, const double *coeffs,
+                           void *stream) {
+  if (!d_src || !d_dst || !coeffs || width < 1 || height < 1) return fail(CYR_ERR_ARGUMENT, "bad warp arguments");
+  const double c[2][3] = {{coeffs[0], coeffs[1], coeffs[2]}, {coeffs[3], coeffs[4], coeffs[5]}};
+  const double det = c[0][0] * c[1][1] - c[0][1] * c[1][0];
+  if (det == 0.0 || !std::isfinite(det)) return fail(CYR_ERR_ARGUMENT, "singular warp matrix");
+  const WarpInverse w = warp_inverse(c);
+  const size_t n = size_t(width) * height;
+  k_warp<<<unsigned((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      d_src, d_dst, width, height, WarpCoef{w.a00, w.a01, w.a02, w.a10, w.a11, w.a12});
+  CYR_CUDA(cudaGetLastError());
+  return CYR_OK;
+}
+
+}  // extern "C"

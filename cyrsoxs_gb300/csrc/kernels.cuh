@@ -1,0 +1,572 @@
+// Device kernels of the GB300 scattering path.
+//
+// Data layout in HBM (all row-major, X fastest, as the reference's voxel
+// index x + y*Nx + z*Nx*Ny, include/uniaxial.h:531-533):
+//   voxels   float4 [M][V]               Voxel::s1 per material
+//   spectra  float2 [nvol][V]            complex volumes (Nt columns or p)
+//   images   float  [A][P]               per-angle Ewald intensity, P = Nx*Ny
+//   avg      float  [P]                  angle average before the detector warp
+//
+// Every kernel is bounds-checked against the sizes it receives; no kernel
+// waits on another block.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cyr {
+
+constexpr int kMaxMaterials = 32;
+constexpr int kMaxAngles = 4096;
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cfma(float s, float2 a, float2 acc) {
+  return make_float2(fmaf(s, a.x, acc.x), fmaf(s, a.y, acc.y));
+}
+
+// ---------------------------------------------------------------------------
+// 1. Dielectric tensor build.
+//
+// Per voxel, summed over materials, the six entries of
+//   Nt = sum_m [ phi_a (A s s^T + B (|s|^2 I - s s^T)) + phi_ui C I ] / 4pi
+// with A = n_par^2 - 1, B = n_perp^2 - 1, C = ((n_par + 2 n_perp)/3)^2 - 1
+// formed in double on the host.  This is the reference's tensor
+// (include/uniaxial.h:94-151 Euler, :218-274 vector) with the identity
+// phi_a|s|^2 + phi_ui - phi = 0 applied exactly (Euler: |s| = 1 and
+// phi = phi_a + phi_ui; vector: phi = phi_ui + |s|^2 by definition, :216),
+// which removes the cancellation of n^2 ~ 1 against phi ~ 1 that limits the
+// reference's FP32 build to ~1e-3.
+// ---------------------------------------------------------------------------
+struct MaterialConsts {
+  float2 A[kMaxMaterials];  // (n_par^2 - 1) / 4pi
+  float2 B[kMaxMaterials];  // (n_perp^2 - 1) / 4pi
+  float2 C[kMaxMaterials];  // (((n_par + 2 n_perp)/3)^2 - 1) / 4pi
+  float2 D[kMaxMaterials];  // (n_par^2 - n_perp^2) / 4pi
+};
+
+struct BuildParams {
+  const float4 *vox;
+  uint32_t nx, ny, nz, nmat;
+  size_t nvox;
+  uint32_t morphology;  // 0 Euler, 1 vector
+  uint32_t mode;        // 0: Nt entries (nvol of them, listed in entry[]); 1: p = R-frame polarization
+  uint32_t nvol;
+  uint32_t entry[6];    // mode 0: Nt entry index (xx xy xz yy yz zz) of each output volume
+  float E[3];           // mode 1: E = R x
+  float Rm[9];          // mode 1: R (row major), for the MATERIAL frame
+  uint32_t material_frame;
+  const float *hann_x, *hann_y, *hann_z;  // null when no windowing
+  float2 *out;          // [nvol][V]
+};
+
+template <int MORPH>
+__device__ __forceinline__ void nt_entries(const BuildParams &p, const MaterialConsts &mc, size_t i, float2 nt[6]) {
+#pragma unroll
+  for (int q = 0; q < 6; ++q) nt[q] = make_float2(0.f, 0.f);
+  for (uint32_t m = 0; m < p.nmat; ++m) {
+    const float4 s = __ldg(&p.vox[m * p.nvox + i]);
+    float sx, sy, sz, pa, pui;
+    if (MORPH == 0) {
+      float st, ct, sp, cp;
+      sincosf(s.y, &st, &ct);
+      sincosf(s.z, &sp, &cp);
+      sx = cp * st;
+      sy = sp * st;
+      sz = ct;
+      pa = s.w * s.x;
+      pui = s.w - pa;
+    } else {
+      sx = s.x, sy = s.y, sz = s.z;
+      pa = 1.f;
+      pui = s.w;
+    }
+    const float xx = sx * sx, yy = sy * sy, zz = sz * sz;
+    const float2 A = mc.A[m], B = mc.B[m], C = mc.C[m], D = mc.D[m];
+    // diagonal: phi_a (A s_i^2 + B (|s|^2 - s_i^2)) + phi_ui C, with |s|^2 - s_i^2 as the reference sums it
+    const float ax = pa * xx, ay = pa * yy, az = pa * zz;
+    const float bx = pa * (yy + zz), by = pa * (xx + zz), bz = pa * (xx + yy);
+    nt[0].x += ax * A.x + bx * B.x + pui * C.x;
+    nt[0].y += ax * A.y + bx * B.y + pui * C.y;
+    nt[3].x += ay * A.x + by * B.x + pui * C.x;
+    nt[3].y += ay * A.y + by * B.y + pui * C.y;
+    nt[5].x += az * A.x + bz * B.x + pui * C.x;
+    nt[5].y += az * A.y + bz * B.y + pui * C.y;
+    const float pxy = pa * sx * sy, pxz = pa * sx * sz, pyz = pa * sy * sz;
+    nt[1] = cfma(pxy, D, nt[1]);
+    nt[2] = cfma(pxz, D, nt[2]);
+    nt[4] = cfma(pyz, D, nt[4]);
+  }
+}
+
+template <int MORPH>
+__global__ void __launch_bounds__(256) k_build(BuildParams p, const MaterialConsts *__restrict__ mcp) {
+  __shared__ MaterialConsts mc;
+  {
+    const float *src = reinterpret_cast<const float *>(mcp);
+    float *dst = reinterpret_cast<float *>(&mc);
+    for (int t = threadIdx.x; t < int(sizeof(MaterialConsts) / 4); t += blockDim.x) dst[t] = src[t];
+  }
+  __syncthreads();
+  const size_t stride = size_t(gridDim.x) * blockDim.x;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
+    float2 nt[6];
+    nt_entries<MORPH>(p, mc, i, nt);
+    float w = 1.f;
+    if (p.hann_x) {
+      const uint32_t x = uint32_t(i % p.nx);
+      const uint32_t y = uint32_t((i / p.nx) % p.ny);
+      const uint32_t z = uint32_t(i / (size_t(p.nx) * p.ny));
+      w = p.hann_x[x] * p.hann_y[y] * p.hann_z[z];
+    }
+    if (p.mode == 0) {
+      for (uint32_t v = 0; v < p.nvol; ++v) p.out[v * p.nvox + i] = cscale(nt[p.entry[v]], w);
+    } else {
+      // p = Nt E (uniaxial.h:106-151), then R^T p in the MATERIAL frame (:163-165)
+      const float e0 = p.E[0], e1 = p.E[1], e2 = p.E[2];
+      float2 q[3];
+      q[0] = cadd(cadd(cscale(nt[0], e0), cscale(nt[1], e1)), cscale(nt[2], e2));
+      q[1] = cadd(cadd(cscale(nt[1], e0), cscale(nt[3], e1)), cscale(nt[4], e2));
+      q[2] = cadd(cadd(cscale(nt[2], e0), cscale(nt[4], e1)), cscale(nt[5], e2));
+      if (p.material_frame) {
+        float2 r[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          r[a] = cadd(cadd(cscale(q[0], p.Rm[0 * 3 + a]), cscale(q[1], p.Rm[1 * 3 + a])), cscale(q[2], p.Rm[2 * 3 + a]));
+        q[0] = r[0], q[1] = r[1], q[2] = r[2];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) p.out[c * p.nvox + i] = cscale(q[c], w);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2. Forward FFT along one axis: shared-memory Stockham autosort, mixed radix
+// {8, 4, 2, 3, 5, 7}, twiddles generated in FP64 on the host (W_N^m table).
+// A block transforms TX lines at once, interleaved in shared memory as
+// [n][TX+1] so that lanes of a warp touch consecutive words.  The X pass
+// loads TX consecutive rows; the Y and Z passes load TX consecutive
+// x-columns, so every global access is a run of TX*8 contiguous bytes or more.
+// Two buffers (ping-pong) make each stage one read and one write per element.
+// ---------------------------------------------------------------------------
+struct FftAxis {
+  uint32_t n;            // line length
+  uint32_t nstages;
+  uint32_t radix[16];
+  const float2 *tw;      // W_n^m, m in [0, n)
+};
+
+__device__ __forceinline__ void dft2(float2 *v) {
+  const float2 a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+__device__ __forceinline__ float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // a * (-i)
+__device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 &v3) {
+  const float2 t0 = cadd(v0, v2), t1 = csub(v0, v2), t2 = cadd(v1, v3), t3 = mul_mi(csub(v1, v3));
+  v0 = cadd(t0, t2);
+  v2 = csub(t0, t2);
+  v1 = cadd(t1, t3);
+  v3 = csub(t1, t3);
+}
+__device__ __forceinline__ void dft8(float2 *v) {
+  float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4(e0, e1, e2, e3);
+  dft4(o0, o1, o2, o3);
+  const float h = 0.70710678118654752440f;
+  o1 = make_float2(h * (o1.x + o1.y), h * (o1.y - o1.x));     // * W8^1 = (1 - i)/sqrt2
+  o2 = mul_mi(o2);                                            // * W8^2 = -i
+  o3 = make_float2(h * (o3.y - o3.x), -h * (o3.x + o3.y));    // * W8^3 = -(1 + i)/sqrt2
+  v[0] = cadd(e0, o0);
+  v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1);
+  v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2);
+  v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3);
+  v[7] = csub(e3, o3);
+}
+// Odd prime radices: direct DFT with cos/sin(2 pi m / R) constants.
+template <int R>
+__device__ __forceinline__ void dft_odd(float2 *v) {
+  float cs[R], sn[R];
+  if (R == 3) {
+    cs[0] = 1.f, sn[0] = 0.f, cs[1] = -0.5f, sn[1] = 0.86602540378443864676f, cs[2] = -0.5f, sn[2] = -0.86602540378443864676f;
+  } else if (R == 5) {
+    const float c1 = 0.30901699437494742410f, s1 = 0.95105651629515357212f;
+    const float c2 = -0.80901699437494742410f, s2 = 0.58778525229247312917f;
+    cs[0] = 1.f, sn[0] = 0.f, cs[1] = c1, sn[1] = s1, cs[2] = c2, sn[2] = s2, cs[3] = c2, sn[3] = -s2, cs[4] = c1,
+    sn[4] = -s1;
+  } else {
+    const float c1 = 0.62348980185873353053f, s1 = 0.78183148246802980871f;
+    const float c2 = -0.22252093395631440429f, s2 = 0.97492791218182360702f;
+    const float c3 = -0.90096886790241912624f, s3 = 0.43388373911755812048f;
+    cs[0] = 1.f, sn[0] = 0.f, cs[1] = c1, sn[1] = s1, cs[2] = c2, sn[2] = s2, cs[3] = c3, sn[3] = s3;
+    cs[4] = c3, sn[4] = -s3, cs[5] = c2, sn[5] = -s2, cs[6] = c1, sn[6] = -s1;
+  }
+  float2 out[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    float2 acc = v[0];
+#pragma unroll
+    for (int j = 1; j < R; ++j) {
+      const int m = (j * q) % R;  // W_R^{jq} = cos - i sin
+      acc.x += v[j].x * cs[m] + v[j].y * sn[m];
+      acc.y += v[j].y * cs[m] - v[j].x * sn[m];
+    }
+    out[q] = acc;
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) v[q] = out[q];
+}
+
+// One Stockham stage of radix R over all lines of the block.
+template <int R>
+__device__ __forceinline__ void stockham_stage(const float2 *__restrict__ src, float2 *__restrict__ dst, uint32_t n,
+                                               uint32_t ns, uint32_t lines, uint32_t S, const float2 *__restrict__ tw) {
+  const uint32_t m = n / R;               // butterflies per line
+  const uint32_t twstep = n / (ns * R);   // W_{ns R}^{k r} = W_n^{k r twstep}
+  const uint32_t jobs = m * lines;
+  for (uint32_t job = threadIdx.x; job < jobs; job += blockDim.x) {
+    const uint32_t l = job % lines, j = job / lines;
+    const uint32_t k = j % ns;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[(j + r * m) * S + l];
+    if (ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[k * r * twstep]));
+    }
+    if (R == 2) dft2(v);
+    if (R == 4) dft4(v[0], v[1], v[2], v[3]);
+    if (R == 8) dft8(v);
+    if (R == 3 || R == 5 || R == 7) dft_odd<(R == 2 || R == 4 || R == 8) ? 3 : R>(v);
+    const uint32_t base = (j / ns) * ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[(base + r * ns) * S + l] = v[r];
+  }
+}
+
+// Runs all stages; returns the buffer holding the result.
+__device__ __forceinline__ float2 *stockham(float2 *a, float2 *b, const FftAxis &ax, uint32_t lines, uint32_t S) {
+  uint32_t ns = 1;
+  for (uint32_t s = 0; s < ax.nstages; ++s) {
+    const uint32_t R = ax.radix[s];
+    switch (R) {
+      case 8: stockham_stage<8>(a, b, ax.n, ns, lines, S, ax.tw); break;
+      case 4: stockham_stage<4>(a, b, ax.n, ns, lines, S, ax.tw); break;
+      case 2: stockham_stage<2>(a, b, ax.n, ns, lines, S, ax.tw); break;
+      case 3: stockham_stage<3>(a, b, ax.n, ns, lines, S, ax.tw); break;
+      case 5: stockham_stage<5>(a, b, ax.n, ns, lines, S, ax.tw); break;
+      default: stockham_stage<7>(a, b, ax.n, ns, lines, S, ax.tw); break;
+    }
+    __syncthreads();
+    float2 *t = a;
+    a = b;
+    b = t;
+    ns *= R;
+  }
+  return a;
+}
+
+// AXIS 0: lines along x (rows).  AXIS 1: along y.  AXIS 2: along z.
+// Grid: x = tiles, y = volume.  TX lines per tile.
+struct FftPassParams {
+  float2 *data;
+  uint32_t nx, ny, nz;
+  size_t nvox;
+  uint32_t tx;  // lines per block
+  FftAxis ax;
+};
+
+template <int AXIS>
+__global__ void __launch_bounds__(256) k_fft_pass(FftPassParams p) {
+  extern __shared__ float2 smem[];
+  const uint32_t n = p.ax.n, TX = p.tx, S = TX + 1;
+  float2 *bufa = smem, *bufb = smem + size_t(n) * S;
+  float2 *vol = p.data + size_t(blockIdx.y) * p.nvox;
+  // Tile geometry: line l of this tile starts at base + l * lstep; element i at + i * estep.
+  size_t base;
+  uint32_t valid;  // number of valid lines in this tile
+  size_t lstep, estep;
+  if (AXIS == 0) {
+    const uint32_t rows = p.ny * p.nz;
+    const uint32_t r0 = blockIdx.x * TX;
+    base = size_t(r0) * p.nx;
+    valid = min(TX, rows - r0);
+    lstep = p.nx;
+    estep = 1;
+  } else {
+    const uint32_t nxt = (p.nx + TX - 1) / TX;
+    const uint32_t xt = blockIdx.x % nxt, other = blockIdx.x / nxt;
+    const uint32_t x0 = xt * TX;
+    valid = min(TX, p.nx - x0);
+    lstep = 1;
+    if (AXIS == 1) {
+      base = size_t(other) * p.nx * p.ny + x0;  // other = z
+      estep = p.nx;
+    } else {
+      base = size_t(other) * p.nx + x0;  // other = y
+      estep = size_t(p.nx) * p.ny;
+    }
+  }
+  const uint32_t total = n * TX;
+  if (AXIS == 0) {
+    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+      const uint32_t l = t / n, i = t % n;
+      bufa[i * S + l] = l < valid ? vol[base + l * lstep + i * estep] : make_float2(0.f, 0.f);
+    }
+  } else {
+    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+      const uint32_t l = t % TX, i = t / TX;
+      bufa[i * S + l] = l < valid ? vol[base + l * lstep + i * estep] : make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();
+  const float2 *res = stockham(bufa, bufb, p.ax, TX, S);
+  if (AXIS == 0) {
+    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+      const uint32_t l = t / n, i = t % n;
+      if (l < valid) vol[base + l * lstep + i * estep] = res[i * S + l];
+    }
+  } else {
+    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+      const uint32_t l = t % TX, i = t / TX;
+      if (l < valid) vol[base + l * lstep + i * estep] = res[i * S + l];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3. DC replacement value per volume (src/cudaMain.cu:123-176): the mean of
+// the periodic neighbours of index 0 in the unshifted spectrum.  The Ewald
+// gather substitutes it wherever it reads index 0; the spectrum itself is
+// left untouched.
+// ---------------------------------------------------------------------------
+__global__ void k_dc(const float2 *__restrict__ spec, uint32_t nvol, size_t nvox, uint32_t nx, uint32_t ny, uint32_t nz,
+                     float2 *__restrict__ dc) {
+  const uint32_t v = threadIdx.x;
+  if (v >= nvol) return;
+  const float2 *P = spec + size_t(v) * nvox;
+  float2 s = make_float2(0.f, 0.f);
+  s = cadd(s, P[1 % nvox]);
+  s = cadd(s, P[nx % nvox]);
+  s = cadd(s, P[(nx - 1) % nvox]);
+  s = cadd(s, P[(size_t(ny - 1) * nx) % nvox]);
+  float cnt = 4.f;
+  if (nz > 1) {
+    s = cadd(s, P[size_t(nx) * ny]);
+    s = cadd(s, P[size_t(nz - 1) * nx * ny]);
+    cnt = 6.f;
+  }
+  dc[v] = make_float2(s.x / cnt, s.y / cnt);
+}
+
+// ---------------------------------------------------------------------------
+// 4. Ewald projection for every E angle at once.
+//
+// Per detector pixel (X, Y): the reference's float geometry
+// (include/uniaxial.h:891-931, with correctly rounded float operations),
+// the spectrum gathered at the Ewald planes through the "Igor" shift
+// j -> (N/2 - j) mod N as index arithmetic (:570-613), the intensity
+// |(k^2 I - Q Q^T) p|^2 (include/cudaUtils.h:268-296) with
+// p = sum_b coef[a][b] * P_b for angle a, and the linear interpolation
+// between the two planes (:800-803).  Writes images[a][P].
+// ---------------------------------------------------------------------------
+struct EwaldParams {
+  const float2 *spec;     // [nvol][V]
+  const float2 *dc;       // [nvol]
+  uint32_t nx, ny, nz;
+  size_t nvox;
+  uint32_t nbasis;        // 1..3
+  uint32_t vol[3][3];     // vol[c][b]: volume holding component c of basis b
+  uint32_t nangles;
+  const float *coef;      // [nangles][nbasis]
+  float start, dx, dy, dz;
+  const float *qx, *qy, *qz;  // q-grid tables (include/uniaxial.h:645-650)
+  float kmag;
+  float kx, ky, kz;       // k * kVector (float)
+  float kvx, kvy, kvz;    // kVector
+  uint32_t interp;        // 0 nearest, 1 linear
+  uint32_t twod;
+  float *images;          // [nangles][P]
+};
+
+__device__ __forceinline__ uint32_t igor(uint32_t j, uint32_t n) {
+  const uint32_t h = n / 2;
+  return j <= h ? h - j : n + h - j;
+}
+
+__device__ __forceinline__ float intensity(float Q0, float Q1, float Q2, float d, float2 p0, float2 p1, float2 p2) {
+  // t = d p - Q (Q . p)
+  const float2 qp = make_float2(Q0 * p0.x + Q1 * p1.x + Q2 * p2.x, Q0 * p0.y + Q1 * p1.y + Q2 * p2.y);
+  const float2 t0 = make_float2(d * p0.x - Q0 * qp.x, d * p0.y - Q0 * qp.y);
+  const float2 t1 = make_float2(d * p1.x - Q1 * qp.x, d * p1.y - Q1 * qp.y);
+  const float2 t2 = make_float2(d * p2.x - Q2 * qp.x, d * p2.y - Q2 * qp.y);
+  return t0.x * t0.x + t0.y * t0.y + t1.x * t1.x + t1.y * t1.y + t2.x * t2.x + t2.y * t2.y;
+}
+
+__global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
+  const size_t npix = size_t(p.nx) * p.ny;
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= npix) return;
+  const uint32_t Y = uint32_t(t / p.nx), X = uint32_t(t % p.nx);
+  // geometry, operation for operation in float with correct rounding
+  const float posx = __fadd_rn(p.start, __fmul_rn(float(X), p.dx));
+  const float posy = __fadd_rn(p.start, __fmul_rn(float(Y), p.dy));
+  const float ax = __fadd_rn(p.kx, posx), ay = __fadd_rn(p.ky, posy);
+  const float val = __fsub_rn(__fsub_rn(__fmul_rn(p.kmag, p.kmag), __fmul_rn(ax, ax)), __fmul_rn(ay, ay));
+  const float nanv = __int_as_float(0x7fc00000);
+  bool isnan_px = (val < 0.f) || (X == p.nx - 1) || (Y == p.ny - 1);
+  uint32_t Z0 = 0, Z1 = 0;
+  float w1 = 0.f;  // weight of plane Z1
+  int nplanes = 1;
+  if (!isnan_px) {
+    const float posz = __fadd_rn(-p.kz, __fsqrt_rn(val));
+    if (p.interp == 0) {
+      if (!p.twod) {
+        const float r = roundf(__fdiv_rn(__fsub_rn(posz, p.start), p.dz));  // round(), uniaxial.h:749
+        Z0 = r <= 0.f ? 0u : uint32_t(r);
+      }
+      if (Z0 > p.nz - 1) isnan_px = true;
+    } else if (!p.twod) {
+      const float tz = __fdiv_rn(__fsub_rn(posz, p.start), p.dz);
+      Z0 = tz <= 0.f ? 0u : uint32_t(tz);
+      if (Z0 >= p.nz - 1) {
+        isnan_px = true;  // Z > Nz-1 is the reference's NaN rule; Z == Nz-1 would read outside the volume
+      } else {
+        Z1 = Z0 + 1;
+        nplanes = 2;
+        const float base = __fadd_rn(p.start, __fmul_rn(float(Z0), p.dz));
+        w1 = __fdiv_rn(__fsub_rn(posz, base), p.dz);
+      }
+    }
+  }
+  float *img = p.images + t;
+  if (isnan_px) {
+    for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
+    return;
+  }
+  // gather the basis spectra at the (one or two) planes
+  const uint32_t ux = igor(X, p.nx), uy = igor(Y, p.ny);
+  float2 P[2][3][3];  // [plane][component][basis]
+  float Q[2][3];
+  const uint32_t zs[2] = {Z0, Z1};
+  for (int pl = 0; pl < nplanes; ++pl) {
+    const uint32_t uz = p.twod ? 0u : igor(zs[pl], p.nz);
+    const size_t idx = size_t(ux) + size_t(uy) * p.nx + size_t(uz) * p.nx * p.ny;
+    for (uint32_t b = 0; b < p.nbasis; ++b)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const uint32_t v = p.vol[c][b];
+        P[pl][c][b] = idx == 0 ? p.dc[v] : __ldg(&p.spec[size_t(v) * p.nvox + idx]);
+      }
+    Q[pl][0] = p.kx + p.qx[X];
+    Q[pl][1] = p.ky + p.qy[Y];
+    Q[pl][2] = p.kz + (p.twod ? 0.f : p.qz[zs[pl]]);
+  }
+  const float d = p.kmag * p.kmag;
+  const float w0 = 1.f - w1;
+  for (uint32_t a = 0; a < p.nangles; ++a) {
+    const float *cf = p.coef + size_t(a) * p.nbasis;
+    float I[2];
+    for (int pl = 0; pl < nplanes; ++pl) {
+      float2 pc[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (uint32_t b = 0; b < p.nbasis; ++b) acc = cfma(cf[b], P[pl][c][b], acc);
+        pc[c] = acc;
+      }
+      I[pl] = intensity(Q[pl][0], Q[pl][1], Q[pl][2], d, pc[0], pc[1], pc[2]);
+    }
+    img[size_t(a) * npix] = nplanes == 2 ? w0 * I[0] + w1 * I[1] : I[0];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 5. Bilinear warp with the semantics of nppiWarpAffine_32f_C1R +
+// NPPI_INTER_LINEAR (src/cudaMain.cu:858, :943): source = A dst in float as
+// fma(a00, x, a01*y) + a02; written only if the source point lies in
+// [0, W-1] x [0, H-1]; neighbours clamped; lerp in fma form.
+// ---------------------------------------------------------------------------
+struct WarpCoef {
+  float a00, a01, a02, a10, a11, a12;
+};
+
+__device__ __forceinline__ bool warp_sample(const float *__restrict__ src, int W, int H, const WarpCoef &c, int xd,
+                                            int yd, float &out) {
+  const float fx_ = float(xd), fy_ = float(yd);
+  const float xs = __fadd_rn(__fmaf_rn(c.a00, fx_, __fmul_rn(c.a01, fy_)), c.a02);
+  const float ys = __fadd_rn(__fmaf_rn(c.a10, fx_, __fmul_rn(c.a11, fy_)), c.a12);
+  if (!(xs >= 0.f && xs <= float(W - 1) && ys >= 0.f && ys <= float(H - 1))) return false;
+  const int x0 = min(int(floorf(xs)), W - 1), y0 = min(int(floorf(ys)), H - 1);
+  const int x1 = min(x0 + 1, W - 1), y1 = min(y0 + 1, H - 1);
+  const float fx = __fsub_rn(xs, float(x0)), fy = __fsub_rn(ys, float(y0));
+  const float A = src[size_t(y0) * W + x0], B = src[size_t(y0) * W + x1];
+  const float C = src[size_t(y1) * W + x0], D = src[size_t(y1) * W + x1];
+  const float gx = __fsub_rn(1.f, fx), gy = __fsub_rn(1.f, fy);
+  const float t0 = __fmaf_rn(gx, A, __fmul_rn(fx, B));
+  const float t1 = __fmaf_rn(gx, C, __fmul_rn(fx, D));
+  out = __fmaf_rn(gy, t0, __fmul_rn(fy, t1));
+  return true;
+}
+
+__global__ void k_warp(const float *__restrict__ src, float *__restrict__ dst, int W, int H, WarpCoef c) {
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= size_t(W) * H) return;
+  float v;
+  if (warp_sample(src, W, H, c, int(t % W), int(t / W), v)) dst[t] = v;
+}
+
+// Rotates every per-angle image, masks and sums over angles in FP64, and
+// averages (src/cudaMain.cu:830-909, include/uniaxial.h:958-992).
+struct RotateParams {
+  const float *images;      // [nangles][P]
+  const WarpCoef *coef;     // [nangles]
+  int W, H;                 // NPP image: width = Ny, height = Nx
+  uint32_t nangles;
+  uint32_t rot_mask;
+  float *avg;               // [P]
+};
+
+__global__ void __launch_bounds__(256) k_rotate_average(RotateParams p) {
+  const size_t npix = size_t(p.W) * p.H;
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= npix) return;
+  const int xd = int(t % p.W), yd = int(t / p.W);
+  double sum = 0.0;
+  uint32_t count = 0;
+  for (uint32_t a = 0; a < p.nangles; ++a) {
+    float v = __int_as_float(0x7fc00000);
+    warp_sample(p.images + size_t(a) * npix, p.W, p.H, p.coef[a], xd, yd, v);
+    if (p.rot_mask) {
+      if (isnan(v)) {
+        v = 0.f;
+      } else {
+        ++count;
+      }
+    }
+    sum += double(v);
+  }
+  float r;
+  if (p.rot_mask) {
+    r = count == 0 ? 0.f : float(sum / double(count));
+  } else {
+    r = float(sum / double(p.nangles));
+  }
+  p.avg[t] = r;
+}
+
+__global__ void k_fill(float *dst, size_t n, float v) {
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = v;
+}
+
+}  // namespace cyr

@@ -1,0 +1,141 @@
+/*
+ * cyrsoxs.h - C ABI of the GB300-native CyRSoXS scattering engine.
+ *
+ * Drop-in boundary for the per-energy, per-E-angle scattering path of
+ * usnistgov/cyrsoxs v1.2.0.0.  Plain C types only: pointers, sizes and a
+ * status code.  Errors never terminate the process (the reference calls
+ * exit(); include/cudaHeaders.h:39-63); they return a non-zero status and
+ * cyr_last_error() describes the failure.
+ *
+ * Array layouts (the reference's own, include/Input/Input.h:35-94,
+ * src/cudaMain.cu:968-971):
+ *   voxels      float[num_material][nz][ny][nx][4]  Voxel::s1 per material,
+ *               Euler (S, theta, psi, Vfrac) or vector (sx, sy, sz, phi_unaligned)
+ *   optical     float[num_energies][num_material][4] (delta_par, beta_par,
+ *               delta_perp, beta_perp); n = 1 - delta + i beta
+ *               (include/PyClass/RefractiveIndex.h:101-106)
+ *   projection  float[num_energies][num_k][ny][nx]
+ *   polarization complex float (re, im) [nz][ny][nx] per component
+ */
+#ifndef CYRSOXS_GB300_H
+#define CYRSOXS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CYR_API __attribute__((visibility("default")))
+#else
+#define CYR_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define CYR_OK 0
+#define CYR_ERR_ARGUMENT 1     /* invalid option or pointer */
+#define CYR_ERR_UNSUPPORTED 2  /* option combination or size not implemented */
+#define CYR_ERR_CUDA 3         /* CUDA runtime error (message in cyr_last_error) */
+#define CYR_ERR_MEMORY 4       /* device memory could not be reserved */
+#define CYR_ERR_NO_DEVICE 5    /* no CUDA device visible */
+#define CYR_ERR_TIMEOUT 6      /* a bounded device wait gave up */
+
+/*
+ * Run options: the fields of the reference's InputData that the scattering
+ * path reads (include/Input/InputData.h:160-232, setters :430-615).
+ */
+typedef struct cyr_options {
+  uint32_t nx, ny, nz;         /* voxelDims[0..2] = X, Y, Z */
+  uint32_t num_material;       /* NUM_MATERIAL (<= 32) */
+  uint32_t num_energies;
+  const float *energies;       /* eV, the order of the optical/projection arrays */
+  float start_angle;           /* E-field rotation, degrees (setEAngles) */
+  float end_angle;
+  float increment_angle;
+  float phys_size;             /* nm */
+  uint32_t case_type;          /* 0 Default, 1 BeamDivergence, 2 GrazingIncidence */
+  uint32_t num_k;              /* number of k vectors (1 for Default) */
+  const float *k_vectors;      /* [num_k][3] unit vectors, as InputData stores them */
+  float detector[3];           /* detectorCoordinates (GrazingIncidence) */
+  uint32_t morphology_type;    /* 0 EulerAngles, 1 VectorMorphology */
+  uint32_t ewald_interpolation;/* 0 NearestNeighbour, 1 Linear */
+  uint32_t windowing;          /* 0 NoPadding, 1 Hanning (Algorithm 0 only) */
+  uint32_t scatter_approach;   /* 0 Partial, 1 Full (numerically identical here) */
+  uint32_t algorithm;          /* 0 CommunicationMinimizing, 1 MemoryMinimizing */
+  uint32_t max_streams;        /* MaxStreams (accepted; the engine schedules itself) */
+  uint32_t rot_mask;           /* RotMask */
+  uint32_t reference_frame;    /* 1 Lab, 0 Material (the reference's bool values) */
+} cyr_options;
+
+/* Human-readable description of the last failure on this thread. */
+CYR_API const char *cyr_last_error(void);
+
+/* Library version string and the number of visible CUDA devices (or -1). */
+CYR_API const char *cyr_version(void);
+CYR_API int cyr_device_count(void);
+
+/*
+ * Full simulation from host buffers (host->device copy, all energies, k
+ * vectors and E angles, device->host copy of the averaged projections).
+ * Replaces cudaMain (include/cudaMain.h:53-60, src/cudaMain.cu:377-1035).
+ */
+CYR_API int cyr_cuda_main(const cyr_options *opt, const float *optical, const float *voxels, float *projection);
+
+/*
+ * Same contract for Algorithm 1 (MemoryMinimizing): replaces cudaMainStreams
+ * (include/cudaMain.h:62-69, src/cudaMain.cu:1037-1667).  Windowing is not
+ * applied, as in the reference.
+ */
+CYR_API int cyr_cuda_main_streams(const cyr_options *opt, const float *optical, const float *voxels, float *projection);
+
+/*
+ * Polarization of one energy (index energy_id) for an E rotation of eangle
+ * RADIANS about the first k vector, before the FFT.  px/py/pz receive
+ * complex float [nz][ny][nx] (re, im interleaved).  Replaces the debug
+ * computePolarization (include/cudaMain.h:71-87, src/cudaMain.cu:1669-1738).
+ */
+CYR_API int cyr_compute_polarization(const cyr_options *opt, const float *optical, const float *voxels, float eangle,
+                             uint32_t energy_id, float *px, float *py, float *pz);
+
+/*
+ * Device-resident variant: voxels and projection are device pointers on the
+ * current device; stream is a cudaStream_t (0 = legacy default stream).  The
+ * call is asynchronous with respect to the host once it returns CYR_OK.
+ * Scratch space is kept by the library between calls (per device).
+ */
+CYR_API int cyr_simulate_device(const cyr_options *opt, const float *optical, const void *d_voxels, float *d_projection,
+                        void *stream);
+
+/* Device bytes the engine needs for one request with these options. */
+CYR_API int cyr_required_device_bytes(const cyr_options *opt, size_t *bytes);
+
+/* Releases the library's cached scratch space on the current device. */
+CYR_API int cyr_release_scratch(void);
+
+/*
+ * Building blocks, exposed for parity tests of the individual stages.
+ * All pointers are device pointers; calls are asynchronous on `stream`.
+ *
+ * cyr_fft3d_device: in-place forward unnormalised 3D DFT of `count`
+ * consecutive complex [nz][ny][nx] volumes (cufftExecC2C FORWARD semantics,
+ * include/cudaMain.h:184-190).
+ */
+CYR_API int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, void *stream);
+
+/*
+ * cyr_warp_affine_device: bilinear affine warp of a float [height][width]
+ * image with the semantics of nppiWarpAffine_32f_C1R + NPPI_INTER_LINEAR
+ * (src/cudaMain.cu:91-121, :858, :943).  coeffs is the 2x3 matrix mapping
+ * source to destination (host memory, row major); d_dst must already hold the
+ * prefill value: pixels whose source falls outside the image keep it.
+ */
+CYR_API int cyr_warp_affine_device(const float *d_src, float *d_dst, int width, int height, const double *coeffs,
+                           void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CYRSOXS_GB300_H */

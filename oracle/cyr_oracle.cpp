@@ -473,7 +473,7 @@ void ewald(const Case &c, const EwaldGeom &g, const cd *P[3], float kmag, F3 kve
       } else {
         const float t0 = (posz - g.start) / g.dz;
         const uint32_t Z = t0 <= 0 ? 0u : static_cast<uint32_t>(t0);  // float -> UINT saturates on the GPU
-        if (Z + 1 > nz - 1) {
+        if (Z >= nz - 1) {
           // Z > Nz-1 is the reference's NaN rule; Z == Nz-1 would make it read
           // plane Nz, outside the volume: the oracle reports NaN there.
           out = std::numeric_limits<double>::quiet_NaN();

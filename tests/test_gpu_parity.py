@@ -1,0 +1,115 @@
+"""GPU parity of the engine, through its C ABI, against the FP64 oracle and the
+reference's own outputs.
+
+Tolerance (the engine's precision contract): over detector pixels above 1e-6
+of the peak, max relative error <= 1e-4 against the FP64 oracle, and NaN
+masks identical to the oracle's and to the reference FP32 build's.
+"""
+import numpy as np
+import pytest
+
+import cases
+import npp_cases
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+GOLDEN = cases.__file__.rsplit("/", 1)[0]
+
+
+def _torch():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def native():
+    _torch()
+    from cyrsoxs_gb300 import _native
+
+    return _native
+
+
+def options_for(case, **over):
+    from cyrsoxs_gb300 import _native
+
+    kv = [[0.0, 0.0, 1.0]] if case.case_type == 0 else [cases._normalize32(k).tolist() for k in case.kvecs]
+    kw = dict(nx=case.nx, ny=case.ny, nz=case.nz, num_material=case.num_material, energies=case.energies,
+              start_angle=case.angles[0], end_angle=case.angles[1], increment_angle=case.angles[2],
+              phys_size=case.phys_size, case_type=case.case_type, k_vectors=kv, detector=case.detector,
+              morphology_type=case.morphology, ewald_interpolation=case.interpolation, windowing=case.windowing,
+              scatter_approach=case.scatter, algorithm=case.algorithm, max_streams=case.max_streams,
+              rot_mask=case.rot_mask, reference_frame=case.frame)
+    kw.update(over)
+    return _native.Options(**kw)
+
+
+def rel_err(a, ref, thr=1e-6):
+    both = ~np.isnan(a) & ~np.isnan(ref)
+    peak = np.abs(ref[both]).max()
+    sel = both & (np.abs(ref) > thr * peak)
+    return np.abs(a[sel] - ref[sel]) / np.abs(ref[sel])
+
+
+@pytest.mark.parametrize("shape,count", [((4, 8, 16), 1), ((7, 15, 20), 2), ((1, 64, 48), 1), ((16, 32, 32), 3),
+                                         ((32, 256, 256), 1), ((9, 25, 49), 1)])
+def test_fft3d_matches_numpy(shape, count):
+    torch = _torch()
+    nat = native()
+    rng = np.random.default_rng(sum(shape) + count)
+    a = (rng.standard_normal((count,) + shape) + 1j * rng.standard_normal((count,) + shape)).astype(np.complex64)
+    d = torch.from_numpy(a.view(np.float32)).cuda()
+    nz, ny, nx = shape
+    nat.fft3d_device(d.data_ptr(), nx, ny, nz, count, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = d.cpu().numpy().view(np.complex64)
+    ref = np.fft.fftn(a.astype(np.complex128), axes=(1, 2, 3))
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err < 2e-6, err
+
+
+def test_warp_is_bit_exact_with_npp_probes():
+    torch = _torch()
+    nat = native()
+    outs = npp_cases.read_outputs(f"{GOLDEN}/npp_warp_out.bin")
+    for i, ((w, h, c, pre, img), ref) in enumerate(zip(npp_cases.probes(), outs)):
+        src = torch.from_numpy(np.ascontiguousarray(img, np.float32)).cuda()
+        dst = torch.full((h, w), pre, dtype=torch.float32, device="cuda")
+        nat.warp_affine_device(src.data_ptr(), dst.data_ptr(), w, h, c, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        got = dst.cpu().numpy()
+        assert np.array_equal(np.isnan(got), np.isnan(ref)), i
+        ok = ~np.isnan(ref)
+        assert np.array_equal(got[ok], ref[ok]), (i, np.abs(got[ok] - ref[ok]).max())
+
+
+PROJ = [n for n, c in cases.CASES.items() if c.mode == 0]
+
+
+@pytest.mark.parametrize("name", PROJ)
+def test_projection_matches_oracle_and_reference(name):
+    nat = native()
+    case = cases.CASES[name]
+    opts = options_for(case)
+    got = nat.cuda_main(opts, cases.optical_constants(case), cases.voxels(case),
+                        streams_variant=case.algorithm == 1).astype(np.float64)
+    want = oracle.run_case(case)
+    r32 = np.fromfile(f"{GOLDEN}/ref_{name}_fp32.bin", np.float32).reshape(want.shape)
+    assert np.array_equal(np.isnan(got), np.isnan(want)), "NaN mask differs from the FP64 oracle"
+    assert np.array_equal(np.isnan(got), np.isnan(r32)), "NaN mask differs from the reference FP32 build"
+    e = rel_err(got, want)
+    assert e.max() <= TOL, e.max()
+
+
+@pytest.mark.parametrize("name", [n for n, c in cases.CASES.items() if c.mode == 1])
+def test_polarization_matches_oracle(name):
+    nat = native()
+    case = cases.CASES[name]
+    opts = options_for(case)
+    eid = int(np.searchsorted(np.asarray(case.energies, np.float32), np.float32(case.pol_energy)))
+    px, py, pz = nat.compute_polarization(opts, cases.optical_constants(case), cases.voxels(case), case.pol_eangle, eid)
+    want = oracle.polarization_case(case)
+    got = np.stack([px, py, pz]).astype(np.complex128)
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
