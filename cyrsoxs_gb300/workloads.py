@@ -1,0 +1,157 @@
+"""Seeded synthetic workloads with the shapes and value distributions of the
+benchmark configurations (no public dataset is involved).
+
+* ``c1``: 2 materials on Z x Y x X = 32 x 256 x 256, physSize 5 nm; material 0
+  is a sphere of radius 40 voxels (vfrac 1 inside) in a matrix of material 1;
+  S = 0.5; theta, psi uniform random per voxel; 280/285/290 eV with
+  delta = beta = 1e-3 + 5e-3 L(E) (Lorentzian at 285 eV, 1 eV wide);
+  E angles 0:15:165.
+* ``c2`` / ``headline``: 4 materials; vfrac from seeded smooth random fields
+  arg-maxed into 4 phases and smoothed over ~3 voxels; S ~ U(0, 1); a smooth
+  random director field (theta = acos n_z, psi = atan2(n_y, n_x)); energies
+  270-300 eV with 2 Lorentzian resonances per material; 36 E angles
+  (0:5:175).  ``c2`` is 128 x 512 x 512 with physSize 2 nm; ``headline`` is
+  the 512^2 x 256 shape (Z x Y x X = 256 x 512 x 512).
+
+Arrays come back in the engine's layout: voxels float32 [M][Z][Y][X][4]
+(Euler s1 = (S, theta, psi, Vfrac)) and optical float32 [E][M][4]
+(delta_par, beta_par, delta_perp, beta_perp).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Workload:
+    name: str
+    nz: int
+    ny: int
+    nx: int
+    num_material: int
+    energies: list
+    angles: tuple
+    phys_size: float
+    seed: int = 0
+    kind: str = "random"  # sphere | random
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nvox(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    def num_angles(self) -> int:
+        s, e, d = self.angles
+        return int(round((e - s) / d + 1)) if abs(e - s) > 1e-6 else 1
+
+
+def _lorentz(e, e0, width):
+    return 1.0 / (1.0 + ((e - e0) / (0.5 * width)) ** 2)
+
+
+def workload(name: str, energies=None) -> Workload:
+    if name == "c1":
+        return Workload("c1", 32, 256, 256, 2, energies or [280.0, 285.0, 290.0], (0.0, 165.0, 15.0), 5.0, 0, "sphere")
+    if name == "c2":
+        es = energies or [float(e) for e in np.linspace(270.0, 300.0, 50)]
+        return Workload("c2", 128, 512, 512, 4, es, (0.0, 175.0, 5.0), 2.0, 2, "random")
+    if name == "headline":
+        es = energies or [float(e) for e in np.linspace(270.0, 300.0, 50)]
+        return Workload("headline", 256, 512, 512, 4, es, (0.0, 175.0, 5.0), 2.0, 7, "random")
+    if name == "small":
+        return Workload("small", 16, 64, 64, 2, energies or [284.0, 286.0], (0.0, 150.0, 30.0), 5.0, 3, "random")
+    raise ValueError(f"unknown workload {name}")
+
+
+def optical_constants(w: Workload) -> np.ndarray:
+    """[E][M][4] float32."""
+    out = np.zeros((len(w.energies), w.num_material, 4), np.float64)
+    if w.kind == "sphere":
+        for i, e in enumerate(w.energies):
+            v = 1e-3 + 5e-3 * _lorentz(e, 285.0, 1.0)
+            out[i, :, :] = v
+        return out.astype(np.float32)
+    rng = np.random.Generator(np.random.PCG64(w.seed + 17))
+    for m in range(w.num_material):
+        e0 = rng.uniform(278.0, 292.0, 2)
+        amp = rng.uniform(2e-3, 8e-3, 2)
+        wid = rng.uniform(0.5, 2.0, 2)
+        aniso = rng.uniform(0.3, 0.9)
+        for i, e in enumerate(w.energies):
+            L = sum(a * _lorentz(e, c, s) for a, c, s in zip(amp, e0, wid))
+            base = 1e-3 * (1 + 0.2 * m)
+            out[i, m] = (base + L, 0.4 * base + 0.5 * L, base + aniso * L, 0.4 * base + 0.5 * aniso * L)
+    return out.astype(np.float32)
+
+
+def _torch_device(prefer_cuda: bool):
+    import torch
+
+    return torch, torch.device("cuda" if (prefer_cuda and torch.cuda.is_available()) else "cpu")
+
+
+def voxels_torch(w: Workload, prefer_cuda: bool = True):
+    """The morphology as a torch float32 tensor [M][Z][Y][X][4] (on the GPU when available)."""
+    torch, dev = _torch_device(prefer_cuda)
+    import torch.nn.functional as F
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(w.seed)
+    M, Z, Y, X = w.num_material, w.nz, w.ny, w.nx
+    out = torch.empty((M, Z, Y, X, 4), dtype=torch.float32, device=dev)
+    if w.kind == "sphere":
+        z = torch.arange(Z, device=dev, dtype=torch.float32).view(Z, 1, 1)
+        y = torch.arange(Y, device=dev, dtype=torch.float32).view(1, Y, 1)
+        x = torch.arange(X, device=dev, dtype=torch.float32).view(1, 1, X)
+        d = torch.sqrt((x - X / 2) ** 2 + (y - Y / 2) ** 2 + (z - Z / 2) ** 2)
+        inside = (d <= 40.0).float()
+        fr = [inside, 1.0 - inside]
+        for m in range(M):
+            out[m, ..., 0] = 0.5
+            out[m, ..., 1] = torch.rand((Z, Y, X), generator=g, device=dev) * math.pi
+            out[m, ..., 2] = torch.rand((Z, Y, X), generator=g, device=dev) * (2 * math.pi)
+            out[m, ..., 3] = fr[m] if m < 2 else 0.0
+        return out
+
+    def smooth(t, k):
+        t = t.view(1, 1, Z, Y, X)
+        for _ in range(2):
+            t = F.avg_pool3d(t, k, stride=1, padding=k // 2, count_include_pad=False)
+        return t.view(Z, Y, X)
+
+    # phases: arg-max of smooth random fields, then smoothed over ~3 voxels
+    best = None
+    label = torch.zeros((Z, Y, X), dtype=torch.int64, device=dev)
+    for m in range(M):
+        f = smooth(torch.randn((Z, Y, X), generator=g, device=dev), 7)
+        if best is None:
+            best = f
+        else:
+            upd = f > best
+            label[upd] = m
+            best = torch.maximum(best, f)
+    del best
+    total = torch.zeros((Z, Y, X), dtype=torch.float32, device=dev)
+    for m in range(M):
+        v = smooth((label == m).float(), 3)
+        out[m, ..., 3] = v
+        total += v
+    out[..., 3] /= total.clamp_min(1e-6)
+    del total, label
+    for m in range(M):
+        out[m, ..., 0] = torch.rand((Z, Y, X), generator=g, device=dev)
+        n = [smooth(torch.randn((Z, Y, X), generator=g, device=dev), 5) for _ in range(3)]
+        norm = torch.sqrt(n[0] ** 2 + n[1] ** 2 + n[2] ** 2).clamp_min(1e-12)
+        nz = (n[2] / norm).clamp(-1.0, 1.0)
+        out[m, ..., 1] = torch.acos(nz)
+        out[m, ..., 2] = torch.atan2(n[1], n[0]) % (2 * math.pi)
+        del n, norm, nz
+    return out
+
+
+def voxels(w: Workload) -> np.ndarray:
+    """The morphology as a numpy float32 array [M][Z][Y][X][4]."""
+    return voxels_torch(w).cpu().numpy()

@@ -275,6 +275,7 @@ struct Case {
   float phys, a0, a1, da, pol_energy, pol_eangle;
   float det[3];
   std::vector<float> energies, kvecs, optical, vox;
+  const float *voxp = nullptr;  // the voxel array in use (vox.data() or caller memory)
 };
 
 Case read_case(const char *path) {
@@ -302,6 +303,7 @@ Case read_case(const char *path) {
   rd(c.optical, size_t(c.ne) * c.nmat * 4);
   rd(c.vox, size_t(c.nmat) * c.nx * c.ny * c.nz * 4);
   if (!in) throw std::runtime_error("truncated case file");
+  c.voxp = c.vox.data();
   return c;
 }
 
@@ -331,7 +333,7 @@ Mat material(const Case &c, size_t e, size_t m) {
 void nt_voxel(const Case &c, const std::vector<Mat> &mats, size_t i, size_t nvox, cd nt[6]) {
   for (int q = 0; q < 6; ++q) nt[q] = 0;
   for (uint32_t m = 0; m < c.nmat; ++m) {
-    const float *s = &c.vox[(m * nvox + i) * 4];
+    const float *s = &c.voxp[(m * nvox + i) * 4];
     const cd npar2 = mats[m].npar * mats[m].npar, nper2 = mats[m].nper * mats[m].nper;
     const cd nsum = mats[m].npar + 2.0 * mats[m].nper;
     const cd nsum2 = nsum * nsum;
@@ -668,6 +670,33 @@ void oracle_set_threads(int n) {
 int oracle_run_case(const char *path, double *out, uint32_t angle_limit, uint32_t energy_limit, double *seconds) {
   try {
     const Case c = read_case(path);
+    const auto t0 = std::chrono::steady_clock::now();
+    simulate(c, out, angle_limit, energy_limit);
+    if (seconds) seconds[0] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// Same pipeline from arrays: hdr = {nx, ny, nz, nmat, ne, nk, morph, window,
+// interp, scatter, rotmask, algo, streams, frame, casetype, mode} (u32[16]),
+// fl = {phys, a0, a1, da, pol_energy, pol_eangle, det0, det1, det2} (f32[9]).
+int oracle_run_arrays(const uint32_t *hdr, const float *fl, const float *energies, const float *kvecs,
+                      const float *optical, const float *voxels, double *out, uint32_t angle_limit,
+                      uint32_t energy_limit, double *seconds) {
+  try {
+    Case c;
+    c.nx = hdr[0], c.ny = hdr[1], c.nz = hdr[2], c.nmat = hdr[3], c.ne = hdr[4], c.nk = hdr[5];
+    c.morph = hdr[6], c.window = hdr[7], c.interp = hdr[8], c.scatter = hdr[9], c.rotmask = hdr[10];
+    c.algo = hdr[11], c.streams = hdr[12], c.frame = hdr[13], c.casetype = hdr[14], c.mode = hdr[15];
+    c.phys = fl[0], c.a0 = fl[1], c.a1 = fl[2], c.da = fl[3], c.pol_energy = fl[4], c.pol_eangle = fl[5];
+    c.det[0] = fl[6], c.det[1] = fl[7], c.det[2] = fl[8];
+    c.energies.assign(energies, energies + c.ne);
+    c.kvecs.assign(kvecs, kvecs + size_t(c.nk) * 3);
+    c.optical.assign(optical, optical + size_t(c.ne) * c.nmat * 4);
+    c.voxp = voxels;
     const auto t0 = std::chrono::steady_clock::now();
     simulate(c, out, angle_limit, energy_limit);
     if (seconds) seconds[0] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -33,6 +33,8 @@ def lib():
         fp = ctypes.POINTER(ctypes.c_float)
         L.oracle_run_case.argtypes = [ctypes.c_char_p, dp, ctypes.c_uint32, ctypes.c_uint32, dp]
         L.oracle_polarization_case.argtypes = [ctypes.c_char_p, dp]
+        u32p = ctypes.POINTER(ctypes.c_uint32)
+        L.oracle_run_arrays.argtypes = [u32p, fp, fp, fp, fp, fp, dp, ctypes.c_uint32, ctypes.c_uint32, dp]
         L.oracle_fft3d.argtypes = [dp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
         L.oracle_warp.argtypes = [dp, dp, ctypes.c_int, ctypes.c_int, dp]
         L.oracle_rotation.argtypes = [fp, ctypes.c_int, ctypes.c_float, fp, fp]
@@ -66,6 +68,30 @@ def run_case(case, angle_limit: int = 0, energy_limit: int = 0):
         _cases.write_case(case, p)
         out, _ = run_case_file(p, _cases.output_shape(case), angle_limit, energy_limit)
     return out
+
+
+def run_arrays(*, nx, ny, nz, energies, optical, voxels, angles, phys_size, morphology=0, windowing=0,
+               interpolation=1, rot_mask=0, algorithm=0, frame=1, case_type=0, kvecs=((0.0, 0.0, 1.0),),
+               detector=(0.0, 0.0, 1.0), angle_limit=0, energy_limit=0):
+    """Pipeline on in-memory arrays (voxels float32 [M][Z][Y][X][4]); returns (out, seconds)."""
+    vox = np.ascontiguousarray(voxels, np.float32)
+    opt = np.ascontiguousarray(optical, np.float32)
+    nmat = vox.shape[0]
+    es = np.ascontiguousarray(energies, np.float32)
+    kv = np.ascontiguousarray(np.asarray(kvecs, np.float32).reshape(-1, 3))
+    hdr = np.array([nx, ny, nz, nmat, es.size, kv.shape[0], morphology, windowing, interpolation, 0, rot_mask,
+                    algorithm, 1, frame, case_type, 0], np.uint32)
+    fl = np.array([phys_size, angles[0], angles[1], angles[2], 0, 0, *detector], np.float32)
+    ne_out = min(energy_limit, es.size) if energy_limit else es.size
+    out = np.full((es.size, kv.shape[0], ny, nx), np.nan, np.float64)
+    secs = np.zeros(1, np.float64)
+    fp = ctypes.POINTER(ctypes.c_float)
+    rc = lib().oracle_run_arrays(hdr.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), fl.ctypes.data_as(fp),
+                                 es.ctypes.data_as(fp), kv.ctypes.data_as(fp), opt.ctypes.data_as(fp),
+                                 vox.ctypes.data_as(fp), _dp(out), angle_limit, energy_limit, _dp(secs))
+    if rc:
+        raise RuntimeError(lib().oracle_last_error().decode())
+    return out[:ne_out], float(secs[0])
 
 
 def polarization_case(case):
