@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 scattering engine: patterns/s on the 512^2 x 256
+morphology (Z x Y x X = 256 x 512 x 512, 4 materials, 36 E angles).
+
+A "pattern" is one Ewald-projected detector image [Ny][Nx] for one
+(energy, k, E angle) - one pass of the reference's angle loop
+(src/cudaMain.cu:611).  A step is one request: ENERGIES_PER_STEP energies of
+the workload, every E angle, through the full path (polarization, 3D FFT, DC
+replacement, shift, Ewald projection, rotation, angle average, detector warp).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+* value: device-resident throughput (morphology already in HBM), timed with
+  CUDA events on the launch stream, max over ranks.  The morphology (4.3 GB)
+  is larger than L2, so no flush is needed between steps.
+* e2e: the same metric through the C ABI call cyr_cuda_main with host buffers
+  (pinned), host->device copy of the morphology and device->host copy of the
+  patterns inside the timed region, wall clock.
+* roofline: per-kernel durations from CUDA events recorded around every
+  launch on its stream during profiled steps; algorithmic bytes per launch as
+  documented in the design doc; peak = measured HBM copy bandwidth.
+* cpu_baseline: the FP64 CPU oracle (restatement of the reference's per-angle
+  algorithm, OpenMP over all host threads) on a bounded sample (1 energy x 2
+  E angles of the same morphology); the same sample checks the engine's
+  precision at full size.
+* --impl reference: the reference's algorithm on the host cores (the
+  reference has no CPU path of its own, so this is the oracle port), one
+  pattern per step.
+Under torchrun, ranks take disjoint energy shards (weak scaling, no data-path
+collective); only the timing uses the process group.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "patterns/s (512²×256, ≤1e-4 rel vs FP64) batched vs plain; p50/p99 latency"
+ENERGIES_PER_STEP = 8
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "c2", "c1", "small"])
+    ap.add_argument("--energies-per-step", type=int, default=ENERGIES_PER_STEP)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--skip-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def shard_energies(all_energies, rank, world, per_rank):
+    """Disjoint, contiguous energy blocks per rank (as src/cudaMain.cu:499-503 splits energies over GPUs)."""
+    need = per_rank * world
+    es = [all_energies[i % len(all_energies)] + 0.001 * (i // len(all_energies)) for i in range(need)]
+    return es[rank * per_rank:(rank + 1) * per_rank]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0, interval_ms=50):
+        self.index, self.interval = index, interval_ms
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", f"-lms={self.interval}"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def load_traffic(workload):
+    """dram bytes per launch of each kernel from the committed ncu summary, or {}."""
+    p = os.path.join(HERE, "profiles", f"traffic_{workload}.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def algorithmic_bytes(kernel, w, nvol, nang, ne_step):
+    """Compulsory bytes per launch (each distinct element read once, written once)."""
+    V, P, M = w.nvox, w.nx * w.ny, w.num_material
+    table = {
+        "k_build": (16 * M + 8 * nvol) * V,
+        "k_fft_pass<x>": 2 * 8 * nvol * V,
+        "k_fft_pass<y>": 2 * 8 * nvol * V,
+        "k_fft_pass<z>": 2 * 8 * nvol * V,
+        "k_ewald_angles": 2 * 8 * nvol * P + 4 * nang * P,
+        "k_rotate_average": 4 * nang * P + 4 * P,
+        "k_fill": 4 * P,
+        "k_warp": 8 * P,
+        "k_dc": 6 * 8 * nvol,
+    }
+    return table.get(kernel)
+
+
+def rel_err(a, ref, thr=1e-6):
+    import numpy as np
+
+    both = ~np.isnan(a) & ~np.isnan(ref)
+    peak = np.abs(ref[both]).max()
+    sel = both & (np.abs(ref) > thr * peak)
+    return float((np.abs(a[sel] - ref[sel]) / np.abs(ref[sel])).max()), int(sel.sum())
+
+
+def run_reference(args):
+    """The reference's algorithm on the host cores: the FP64 oracle port, all threads, one pattern per step."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    from cyrsoxs_gb300 import workloads
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+
+    oracle.build()
+    w = workloads.workload(args.workload)
+    vox = workloads.voxels(w)
+    opt_all = workloads.optical_constants(w)
+    cores = oracle.num_threads()
+    times = []
+    for s in range(args.warmup + args.steps):
+        e = s % len(w.energies)
+        _, secs = oracle.run_arrays(nx=w.nx, ny=w.ny, nz=w.nz, energies=[w.energies[e]], optical=opt_all[e:e + 1],
+                                    voxels=vox, angles=w.angles, phys_size=w.phys_size, angle_limit=1,
+                                    energy_limit=1)
+        if s >= args.warmup:
+            times.append(secs)
+    total = sum(times)
+    value = len(times) / total
+    line = {
+        "metric": METRIC, "value": value, "unit": "patterns/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic (seeded morphology with the configuration's shapes and distributions)",
+        "config": {"workload": f"{w.name}: Z x Y x X = {w.nz} x {w.ny} x {w.nx}, {w.num_material} materials, "
+                               f"{w.num_angles()} E angles", "sample": "1 energy x 1 E angle per step"},
+        "cpu_baseline": {"value": value, "unit": "patterns/s", "cores": cores, "kind": "port",
+                         "sample": "1 energy x 1 E angle of the workload per step (per-angle algorithm, FP64)"},
+        "e2e": {"value": value, "unit": "patterns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    if world != args.gpus:
+        print(f"warning: --gpus {args.gpus} but WORLD_SIZE {world}", file=sys.stderr)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from cyrsoxs_gb300 import _native, workloads
+
+    w = workloads.workload(args.workload)
+    nang = w.num_angles()
+    energies = shard_energies(w.energies, rank, world, args.energies_per_step)
+    wstep = workloads.workload(args.workload, energies=energies)
+    optical = workloads.optical_constants(wstep)
+    vox = workloads.voxels_torch(w).contiguous()
+    opts = _native.Options(nx=w.nx, ny=w.ny, nz=w.nz, num_material=w.num_material, energies=energies,
+                           start_angle=w.angles[0], end_angle=w.angles[1], increment_angle=w.angles[2],
+                           phys_size=w.phys_size, morphology_type=0)
+    P = w.nx * w.ny
+    out = torch.empty(len(energies) * P, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def step():
+        _native.simulate_device(opts, optical, vox.data_ptr(), out.data_ptr(), sptr)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # timed region: device-resident throughput
+    step_ms = []
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    total_ms = t0.elapsed_time(t1)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    patterns = world * len(energies) * nang * args.steps
+    value = patterns / (total_ms / 1000.0)
+
+    # per-kernel durations (events around every launch on its stream)
+    prof_steps = max(1, min(args.steps, 5))
+    _native.profile_begin(4096)
+    for _ in range(prof_steps):
+        step()
+    torch.cuda.synchronize()
+    kernels, dropped = _native.profile_end()
+    launches_per_step = sum(n for n, _ in kernels.values()) / prof_steps
+    nvol = 5
+    dom = max(kernels.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_n, dom_ms) = dom
+    peak, peak_kind = load_peaks()
+    dom_bytes = algorithmic_bytes(dom_name, w, nvol, nang, len(energies))
+    achieved = dom_bytes / (dom_ms / dom_n / 1000.0) / 1e9
+    traffic = load_traffic(w.name).get(dom_name)
+    kernel_table = {k: {"launches_per_step": n / prof_steps, "ms_per_launch": ms / n,
+                        "gbs": (algorithmic_bytes(k, w, nvol, nang, len(energies)) or 0) / (ms / n / 1000.0) / 1e9}
+                    for k, (n, ms) in kernels.items()}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "patterns/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded morphology with the configuration's shapes and distributions)",
+        "config": {"workload": f"{w.name}: Z x Y x X = {w.nz} x {w.ny} x {w.nx}, {w.num_material} materials (Euler), "
+                               f"{nang} E angles (0:5:175), {len(energies)} energies per step per GPU, physSize "
+                               f"{w.phys_size} nm, k = z",
+                   "path": "plain (one request at a time, device-resident morphology)",
+                   "l2": "inputs larger than L2 (morphology 4.3 GB)",
+                   "patterns_per_step": world * len(energies) * nang},
+        "latency_ms": {"p50_step": statistics.median(step_ms),
+                       "p99_step": sorted(step_ms)[min(len(step_ms) - 1, int(math.ceil(0.99 * len(step_ms))) - 1)]},
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": dom_bytes},
+        "kernels": kernel_table,
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "clocks": None,
+    }
+    if rank == 0:
+        result["clocks"] = clocks.summary()
+
+    # e2e through the C ABI with host buffers (pinned), copies inside the timed region
+    host_vox = torch.empty(vox.shape, dtype=torch.float32, pin_memory=True)
+    host_vox.copy_(vox)
+    host_vox_np = host_vox.numpy()
+    del vox, out
+    torch.cuda.empty_cache()
+    host_out = torch.empty((len(energies), 1, w.ny, w.nx), dtype=torch.float32, pin_memory=True).numpy()
+    _native.cuda_main(opts, optical, host_vox_np)  # warm (scratch allocation)
+    e2e_times = []
+    barrier()
+    for _ in range(args.e2e_steps):
+        t = time.perf_counter()
+        _native.cuda_main(opts, optical, host_vox_np, out=host_out)
+        e2e_times.append(time.perf_counter() - t)
+    barrier()
+    e2e_s = sum(e2e_times)
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    result["e2e"] = {"value": world * len(energies) * nang * args.e2e_steps / e2e_s, "unit": "patterns/s",
+                     "h2d_bytes_per_step": int(host_vox_np.nbytes + optical.nbytes),
+                     "d2h_bytes_per_step": int(host_out.nbytes), "steps": args.e2e_steps,
+                     "api": "cyr_cuda_main (host buffers)"}
+
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        sys.path.insert(0, os.path.join(HERE, "oracle"))
+        import oracle
+
+        oracle.build()
+        two = (w.angles[0], w.angles[0] + w.angles[2], w.angles[2])
+        o2 = _native.Options(nx=w.nx, ny=w.ny, nz=w.nz, num_material=w.num_material, energies=energies[:1],
+                             start_angle=two[0], end_angle=two[1], increment_angle=two[2], phys_size=w.phys_size)
+        gpu2 = _native.cuda_main(o2, optical[:1], host_vox_np).astype(np.float64)
+        ref2, secs = oracle.run_arrays(nx=w.nx, ny=w.ny, nz=w.nz, energies=energies[:1], optical=optical[:1],
+                                       voxels=host_vox_np, angles=two, phys_size=w.phys_size)
+        err, npx = rel_err(gpu2, ref2)
+        result["cpu_baseline"] = {"value": 2.0 / secs, "unit": "patterns/s", "cores": oracle.num_threads(),
+                                  "kind": "port", "seconds": secs,
+                                  "sample": "1 energy x 2 E angles of the same morphology (per-angle algorithm, FP64)"}
+        result["precision"] = {"max_rel_err_vs_fp64": err, "pixels": npx,
+                               "nan_mask_equal": bool(np.array_equal(np.isnan(gpu2), np.isnan(ref2))),
+                               "sample": "1 energy x 2 E angles, full-size morphology, pixels above 1e-6 of peak"}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

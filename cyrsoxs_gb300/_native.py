@@ -79,6 +79,12 @@ def lib():
                                    ctypes.c_uint32, ctypes.c_void_p]
     L.cyr_warp_affine_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+    L.cyr_profile_begin.argtypes = [ctypes.c_uint32]
+    L.cyr_profile_end.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
+                                  ctypes.POINTER(ctypes.c_uint32)]
+    L.cyr_stage_name.argtypes = [ctypes.c_uint32]
+    L.cyr_stage_name.restype = ctypes.c_char_p
+    L.cyr_num_stages.restype = ctypes.c_uint32
     _lib = L
     return L
 
@@ -132,10 +138,14 @@ class Options:
         return int(self.struct.num_k)
 
 
-def cuda_main(opts: Options, optical: np.ndarray, voxels: np.ndarray, streams_variant: bool = False) -> np.ndarray:
-    """Full simulation from host arrays -> float32 [E][K][ny][nx]."""
+def cuda_main(opts: Options, optical: np.ndarray, voxels: np.ndarray, streams_variant: bool = False,
+              out: np.ndarray | None = None) -> np.ndarray:
+    """Full simulation from host arrays -> float32 [E][K][ny][nx] (written into `out` when given)."""
     s = opts.struct
-    out = np.empty((s.num_energies, opts.num_k, s.ny, s.nx), np.float32)
+    shape = (s.num_energies, opts.num_k, s.ny, s.nx)
+    if out is None:
+        out = np.empty(shape, np.float32)
+    assert out.shape == shape and out.dtype == np.float32 and out.flags.c_contiguous
     fn = lib().cyr_cuda_main_streams if streams_variant else lib().cyr_cuda_main
     check(fn(opts.ref, fptr(np.ascontiguousarray(optical, np.float32)), fptr(np.ascontiguousarray(voxels, np.float32)),
              fptr(out)))
@@ -172,6 +182,24 @@ def warp_affine_device(d_src: int, d_dst: int, width: int, height: int, coeffs, 
     c = np.ascontiguousarray(np.asarray(coeffs, np.float64).reshape(6))
     check(lib().cyr_warp_affine_device(ctypes.c_void_p(d_src), ctypes.c_void_p(d_dst), width, height,
                                        c.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_void_p(stream)))
+
+
+def profile_begin(max_launches: int = 65536) -> None:
+    check(lib().cyr_profile_begin(int(max_launches)))
+
+
+def profile_end():
+    """{kernel name: (launches, total ms)} for the launches since profile_begin, and the dropped count."""
+    n = int(lib().cyr_num_stages())
+    launches = (ctypes.c_uint32 * n)()
+    ms = (ctypes.c_double * n)()
+    dropped = ctypes.c_uint32(0)
+    check(lib().cyr_profile_end(launches, ms, n, ctypes.byref(dropped)))
+    out = {}
+    for i in range(n):
+        if launches[i]:
+            out[lib().cyr_stage_name(i).decode()] = (int(launches[i]), float(ms[i]))
+    return out, int(dropped.value)
 
 
 def device_count() -> int:

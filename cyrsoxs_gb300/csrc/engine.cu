@@ -117,8 +117,36 @@ struct DeviceBuffer {
   }
 };
 
+// Optional per-launch timing: an event pair around every kernel launch,
+// read back after the caller has synchronised (cyr_profile_end).
+enum Stage { kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kNumStages };
+const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_pass<y>", "k_fft_pass<z>", "k_dc",
+                                             "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp"};
+
+struct Profiler {
+  bool active = false;
+  std::vector<cudaEvent_t> events;  // pairs
+  std::vector<int> stage;           // stage of pair i
+  size_t used = 0;                  // pairs recorded
+  size_t dropped = 0;
+  int begin(int st, cudaStream_t s) {
+    if (!active) return -1;
+    if (used >= stage.size()) {
+      ++dropped;
+      return -1;
+    }
+    stage[used] = st;
+    cudaEventRecord(events[2 * used], s);
+    return int(used++);
+  }
+  void end(int slot, cudaStream_t s) {
+    if (slot >= 0) cudaEventRecord(events[2 * size_t(slot) + 1], s);
+  }
+};
+
 struct DeviceContext {
   int device = -1;
+  Profiler prof;
   std::mutex mu;
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
@@ -209,9 +237,11 @@ int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t n
       tiles = nxt * (axis == 1 ? nz : ny);
     }
     const dim3 grid(tiles, count);
+    const int slot = ctx.prof.begin(kFftX + axis, st);
     if (axis == 0) k_fft_pass<0><<<grid, 256, smem, st>>>(p);
     if (axis == 1) k_fft_pass<1><<<grid, 256, smem, st>>>(p);
     if (axis == 2) k_fft_pass<2><<<grid, 256, smem, st>>>(p);
+    ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
   }
   return CYR_OK;
@@ -482,13 +512,17 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       bp.mode = 0;
       bp.nvol = pl.nvol;
       for (uint32_t v = 0; v < 6; ++v) bp.entry[v] = v;
+      int slot = ctx.prof.begin(kBuild, st);
       if (o->morphology_type == 0)
         k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
       else
         k_build<1><<<build_blocks, 256, 0, st>>>(bp, mce);
+      ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());
       CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, pl.nvol, st));
+      slot = ctx.prof.begin(kDc, st);
       k_dc<<<1, 32, 0, st>>>(spec, pl.nvol, pl.nvox, pl.nx, pl.ny, pl.nz, dc);
+      ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());
     }
     for (uint32_t k = 0; k < pl.nk; ++k) {
@@ -499,7 +533,9 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
         ep.nangles = pl.nang;
         ep.coef = dcoef + size_t(k) * pl.nang * pl.nbasis;
         ep.images = images;
+        const int slot = ctx.prof.begin(kEwald, st);
         k_ewald_angles<<<pix_blocks, 256, 0, st>>>(ep);
+        ctx.prof.end(slot, st);
         CYR_CUDA(cudaGetLastError());
       } else {
         // per-angle schedule: p(angle) -> FFT -> DC -> Ewald into image slot a
@@ -510,17 +546,23 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
           bp.material_frame = 1;
           for (int c = 0; c < 3; ++c) bp.E[c] = pl.evec[ka * 3 + c];
           std::memcpy(bp.Rm, pl.rmats[ka].m, sizeof bp.Rm);
+          int slot = ctx.prof.begin(kBuild, st);
           if (o->morphology_type == 0)
             k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
           else
             k_build<1><<<build_blocks, 256, 0, st>>>(bp, mce);
+          ctx.prof.end(slot, st);
           CYR_CUDA(cudaGetLastError());
           CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, 3, st));
+          slot = ctx.prof.begin(kDc, st);
           k_dc<<<1, 32, 0, st>>>(spec, 3, pl.nvox, pl.nx, pl.ny, pl.nz, dc);
+          ctx.prof.end(slot, st);
           ep.nangles = 1;
           ep.coef = dcoef + ka;  // nbasis == 1, coefficient 1
           ep.images = images + size_t(a) * pl.npix;
+          slot = ctx.prof.begin(kEwald, st);
           k_ewald_angles<<<pix_blocks, 256, 0, st>>>(ep);
+          ctx.prof.end(slot, st);
           CYR_CUDA(cudaGetLastError());
         }
       }
@@ -531,11 +573,17 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       rp.nangles = pl.nang;
       rp.rot_mask = o->rot_mask;
       rp.avg = avg;
+      int slot = ctx.prof.begin(kRotate, st);
       k_rotate_average<<<pix_blocks, 256, 0, st>>>(rp);
+      ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());
       float *dst = d_out + (size_t(e) * pl.nk + k) * pl.npix;
+      slot = ctx.prof.begin(kFill, st);
       k_fill<<<pix_blocks, 256, 0, st>>>(dst, pl.npix, o->rot_mask ? 0.f : std::numeric_limits<float>::quiet_NaN());
+      ctx.prof.end(slot, st);
+      slot = ctx.prof.begin(kWarp, st);
       k_warp<<<pix_blocks, 256, 0, st>>>(avg, dst, W, H, pl.detector_warp[k]);
+      ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());
     }
   }
@@ -707,6 +755,53 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
   cudaStreamDestroy(st);
   return rc;
 }
+
+int cyr_profile_begin(uint32_t max_launches) {
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  Profiler &p = ctx->prof;
+  const size_t want = std::max<uint32_t>(max_launches, 1);
+  while (p.events.size() < 2 * want) {
+    cudaEvent_t e;
+    CYR_CUDA(cudaEventCreate(&e));
+    p.events.push_back(e);
+  }
+  p.stage.assign(want, -1);
+  p.used = 0;
+  p.dropped = 0;
+  p.active = true;
+  return CYR_OK;
+}
+
+int cyr_profile_end(uint32_t *launches, double *ms, uint32_t nstages, uint32_t *dropped) {
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  Profiler &p = ctx->prof;
+  p.active = false;
+  for (uint32_t i = 0; i < nstages; ++i) {
+    if (launches) launches[i] = 0;
+    if (ms) ms[i] = 0.0;
+  }
+  for (size_t i = 0; i < p.used; ++i) {
+    float t = 0.f;
+    CYR_CUDA(cudaEventSynchronize(p.events[2 * i + 1]));
+    CYR_CUDA(cudaEventElapsedTime(&t, p.events[2 * i], p.events[2 * i + 1]));
+    const int s = p.stage[i];
+    if (s >= 0 && uint32_t(s) < nstages) {
+      if (launches) launches[s] += 1;
+      if (ms) ms[s] += t;
+    }
+  }
+  if (dropped) *dropped = uint32_t(p.dropped);
+  p.used = 0;
+  return CYR_OK;
+}
+
+const char *cyr_stage_name(uint32_t stage) { return stage < kNumStages ? kStageNames[stage] : ""; }
+
+uint32_t cyr_num_stages(void) { return kNumStages; }
 
 int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, void *stream) {
   if (!d_data || nx < 1 || ny < 1 || nz < 1 || count < 1) return fail(CYR_ERR_ARGUMENT, "bad FFT arguments");

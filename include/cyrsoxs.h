@@ -134,6 +134,19 @@ CYR_API int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz
 CYR_API int cyr_warp_affine_device(const float *d_src, float *d_dst, int width, int height, const double *coeffs,
                            void *stream);
 
+/*
+ * Per-kernel timing.  Between cyr_profile_begin and cyr_profile_end every
+ * kernel the engine launches is bracketed by a pair of CUDA events recorded
+ * on its launch stream (no synchronisation is added).  cyr_profile_end waits
+ * for the recorded events and returns, per kernel kind (cyr_stage_name), the
+ * number of launches and their summed duration in milliseconds.  Launches
+ * beyond max_launches are counted in *dropped and not timed.
+ */
+CYR_API int cyr_profile_begin(uint32_t max_launches);
+CYR_API int cyr_profile_end(uint32_t *launches, double *ms, uint32_t nstages, uint32_t *dropped);
+CYR_API const char *cyr_stage_name(uint32_t stage);
+CYR_API uint32_t cyr_num_stages(void);
+
 #ifdef __cplusplus
 }
 #endif
