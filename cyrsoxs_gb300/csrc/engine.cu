@@ -84,8 +84,10 @@ bool factorize(uint32_t n, std::vector<uint32_t> &radix) {
 
 constexpr size_t kFftSmemBudget = 200 * 1024;
 
+// Lines per block: about 4096 elements per tile, at most 16 lines.
 uint32_t fft_lines_per_block(uint32_t n) {
   uint32_t tx = 16;
+  while (tx > 1 && size_t(n) * tx > 4096) tx /= 2;
   while (tx > 1 && size_t(2) * n * (tx + 1) * sizeof(float2) > kFftSmemBudget) tx /= 2;
   return tx;
 }
@@ -119,9 +121,10 @@ struct DeviceBuffer {
 
 // Optional per-launch timing: an event pair around every kernel launch,
 // read back after the caller has synchronised (cyr_profile_end).
-enum Stage { kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kNumStages };
+enum Stage { kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kNumStages };
 const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_pass<y>", "k_fft_pass<z>", "k_dc",
-                                             "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp"};
+                                             "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp",
+                                             "k_moments", "k_entry_means"};
 
 struct Profiler {
   bool active = false;
@@ -150,7 +153,7 @@ struct DeviceContext {
   std::mutex mu;
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
-  DeviceBuffer spec, images, avg, params, dc, vox_in, out_in;
+  DeviceBuffer spec, images, avg, params, dc, vox_in, out_in, moments, means;
   cudaEvent_t last_use = nullptr;  // completion of the last request that used the scratch
 };
 
@@ -210,7 +213,8 @@ int make_axis(DeviceContext &ctx, uint32_t n, FftAxis &ax) {
   if (!factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u has a prime factor above 7", n);
   ax.n = n;
   ax.nstages = uint32_t(r.size());
-  for (size_t i = 0; i < r.size(); ++i) ax.radix[i] = r[i];
+  ax.radix_code = 0;
+  for (size_t i = 0; i < r.size(); ++i) ax.radix_code |= uint64_t(r[i]) << (4 * i);
   return get_twiddles(ctx, n, &ax.tw);
 }
 
@@ -238,9 +242,9 @@ int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t n
     }
     const dim3 grid(tiles, count);
     const int slot = ctx.prof.begin(kFftX + axis, st);
-    if (axis == 0) k_fft_pass<0><<<grid, 256, smem, st>>>(p);
-    if (axis == 1) k_fft_pass<1><<<grid, 256, smem, st>>>(p);
-    if (axis == 2) k_fft_pass<2><<<grid, 256, smem, st>>>(p);
+    if (axis == 0) k_fft_pass<0><<<grid, kFftThreads, smem, st>>>(p);
+    if (axis == 1) k_fft_pass<1><<<grid, kFftThreads, smem, st>>>(p);
+    if (axis == 2) k_fft_pass<2><<<grid, kFftThreads, smem, st>>>(p);
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
   }
@@ -475,6 +479,38 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   CYR_TRY(ctx.params.ensure(pl.arena.size()));
   CYR_CUDA(cudaMemcpyAsync(ctx.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
   const unsigned char *dp = ctx.params.as<unsigned char>();
+  // volume moments of the morphology -> mean of every tensor entry, per energy
+  CYR_TRY(ctx.moments.ensure(size_t(pl.nmat) * kMoments * sizeof(double)));
+  CYR_TRY(ctx.means.ensure(size_t(pl.ne) * 6 * sizeof(float2)));
+  CYR_CUDA(cudaMemsetAsync(ctx.moments.ptr, 0, size_t(pl.nmat) * kMoments * sizeof(double), st));
+  {
+    MomentParams mp{};
+    mp.vox = d_vox;
+    mp.nx = pl.nx, mp.ny = pl.ny, mp.nz = pl.nz, mp.nmat = pl.nmat;
+    mp.nvox = pl.nvox;
+    if (pl.hanning) {
+      mp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
+      mp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
+      mp.hann_z = reinterpret_cast<const float *>(dp + pl.off_hz);
+    }
+    mp.out = ctx.moments.as<double>();
+    int nsm = 0;
+    CYR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx.device));
+    const dim3 grid(uint32_t(std::max<size_t>(1, std::min<size_t>((pl.nvox + 255) / 256, size_t(nsm) * 8))), pl.nmat);
+    int slot = ctx.prof.begin(kMom, st);
+    if (o->morphology_type == 0)
+      k_moments<0><<<grid, 256, 0, st>>>(mp);
+    else
+      k_moments<1><<<grid, 256, 0, st>>>(mp);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+    slot = ctx.prof.begin(kMeans, st);
+    k_entry_means<<<1, 64, 0, st>>>(ctx.moments.as<double>(), pl.nmat, pl.nvox,
+                                    reinterpret_cast<const MaterialConsts *>(dp + pl.off_mc), pl.ne,
+                                    ctx.means.as<float2>());
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+  }
   float2 *spec = ctx.spec.as<float2>();
   float2 *dc = ctx.dc.as<float2>();
   float *images = ctx.images.as<float>();
@@ -511,7 +547,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       // tensor entries once per energy: xx xy xz yy yz [zz]
       bp.mode = 0;
       bp.nvol = pl.nvol;
-      for (uint32_t v = 0; v < 6; ++v) bp.entry[v] = v;
+      bp.mean = ctx.means.as<float2>() + size_t(e) * 6;
       int slot = ctx.prof.begin(kBuild, st);
       if (o->morphology_type == 0)
         k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
@@ -544,6 +580,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
           bp.mode = 1;
           bp.nvol = 3;
           bp.material_frame = 1;
+          bp.mean = ctx.means.as<float2>() + size_t(e) * 6;
           for (int c = 0; c < 3; ++c) bp.E[c] = pl.evec[ka * 3 + c];
           std::memcpy(bp.Rm, pl.rmats[ka].m, sizeof bp.Rm);
           int slot = ctx.prof.begin(kBuild, st);
@@ -634,6 +671,8 @@ int cyr_release_scratch(void) {
   ctx->avg.release();
   ctx->params.release();
   ctx->dc.release();
+  ctx->moments.release();
+  ctx->means.release();
   ctx->vox_in.release();
   ctx->out_in.release();
   return CYR_OK;

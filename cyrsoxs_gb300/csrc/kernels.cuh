@@ -54,9 +54,9 @@ struct BuildParams {
   uint32_t nx, ny, nz, nmat;
   size_t nvox;
   uint32_t morphology;  // 0 Euler, 1 vector
-  uint32_t mode;        // 0: Nt entries (nvol of them, listed in entry[]); 1: p = R-frame polarization
-  uint32_t nvol;
-  uint32_t entry[6];    // mode 0: Nt entry index (xx xy xz yy yz zz) of each output volume
+  uint32_t mode;        // 0: tensor entries; 1: p = R-frame polarization
+  uint32_t nvol;        // mode 0: entries xx xy xz yy yz [zz] written in this order
+  const float2 *mean;   // [6] volume mean of each windowed entry (null: none subtracted)
   float E[3];           // mode 1: E = R x
   float Rm[9];          // mode 1: R (row major), for the MATERIAL frame
   uint32_t material_frame;
@@ -64,42 +64,138 @@ struct BuildParams {
   float2 *out;          // [nvol][V]
 };
 
+// Direction and fractions of one material at one voxel.
+template <int MORPH>
+__device__ __forceinline__ void director(float4 s, float &sx, float &sy, float &sz, float &pa, float &pui) {
+  if (MORPH == 0) {  // Euler: s1 = (S, theta, psi, Vfrac), uniaxial.h:82-92
+    float st, ct, sp, cp;
+    sincosf(s.y, &st, &ct);
+    sincosf(s.z, &sp, &cp);
+    sx = cp * st;
+    sy = sp * st;
+    sz = ct;
+    pa = s.w * s.x;
+    pui = s.w - pa;
+  } else {  // vector: s1 = (sx, sy, sz, phi_unaligned), uniaxial.h:207-216
+    sx = s.x, sy = s.y, sz = s.z;
+    pa = 1.f;
+    pui = s.w;
+  }
+}
+
 template <int MORPH>
 __device__ __forceinline__ void nt_entries(const BuildParams &p, const MaterialConsts &mc, size_t i, float2 nt[6]) {
 #pragma unroll
   for (int q = 0; q < 6; ++q) nt[q] = make_float2(0.f, 0.f);
-  for (uint32_t m = 0; m < p.nmat; ++m) {
-    const float4 s = __ldg(&p.vox[m * p.nvox + i]);
-    float sx, sy, sz, pa, pui;
-    if (MORPH == 0) {
-      float st, ct, sp, cp;
-      sincosf(s.y, &st, &ct);
-      sincosf(s.z, &sp, &cp);
-      sx = cp * st;
-      sy = sp * st;
-      sz = ct;
-      pa = s.w * s.x;
-      pui = s.w - pa;
-    } else {
-      sx = s.x, sy = s.y, sz = s.z;
-      pa = 1.f;
-      pui = s.w;
+  for (uint32_t m0 = 0; m0 < p.nmat; m0 += 4) {
+    float4 sv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)  // issue the loads of up to 4 materials before using them
+      if (m0 + u < p.nmat) sv[u] = __ldg(&p.vox[(m0 + u) * p.nvox + i]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (m0 + u >= p.nmat) break;
+      const uint32_t m = m0 + u;
+      float sx, sy, sz, pa, pui;
+      director<MORPH>(sv[u], sx, sy, sz, pa, pui);
+      const float xx = sx * sx, yy = sy * sy, zz = sz * sz;
+      const float2 A = mc.A[m], B = mc.B[m], C = mc.C[m], D = mc.D[m];
+      // diagonal: phi_a (A s_i^2 + B (|s|^2 - s_i^2)) + phi_ui C, with |s|^2 - s_i^2 as the reference sums it
+      const float ax = pa * xx, ay = pa * yy, az = pa * zz;
+      const float bx = pa * (yy + zz), by = pa * (xx + zz), bz = pa * (xx + yy);
+      nt[0].x += ax * A.x + bx * B.x + pui * C.x;
+      nt[0].y += ax * A.y + bx * B.y + pui * C.y;
+      nt[3].x += ay * A.x + by * B.x + pui * C.x;
+      nt[3].y += ay * A.y + by * B.y + pui * C.y;
+      nt[5].x += az * A.x + bz * B.x + pui * C.x;
+      nt[5].y += az * A.y + bz * B.y + pui * C.y;
+      const float pxy = pa * sx * sy, pxz = pa * sx * sz, pyz = pa * sy * sz;
+      nt[1] = cfma(pxy, D, nt[1]);
+      nt[2] = cfma(pxz, D, nt[2]);
+      nt[4] = cfma(pyz, D, nt[4]);
     }
-    const float xx = sx * sx, yy = sy * sy, zz = sz * sz;
-    const float2 A = mc.A[m], B = mc.B[m], C = mc.C[m], D = mc.D[m];
-    // diagonal: phi_a (A s_i^2 + B (|s|^2 - s_i^2)) + phi_ui C, with |s|^2 - s_i^2 as the reference sums it
-    const float ax = pa * xx, ay = pa * yy, az = pa * zz;
-    const float bx = pa * (yy + zz), by = pa * (xx + zz), bz = pa * (xx + yy);
-    nt[0].x += ax * A.x + bx * B.x + pui * C.x;
-    nt[0].y += ax * A.y + bx * B.y + pui * C.y;
-    nt[3].x += ay * A.x + by * B.x + pui * C.x;
-    nt[3].y += ay * A.y + by * B.y + pui * C.y;
-    nt[5].x += az * A.x + bz * B.x + pui * C.x;
-    nt[5].y += az * A.y + bz * B.y + pui * C.y;
-    const float pxy = pa * sx * sy, pxz = pa * sx * sz, pyz = pa * sy * sz;
-    nt[1] = cfma(pxy, D, nt[1]);
-    nt[2] = cfma(pxz, D, nt[2]);
-    nt[4] = cfma(pyz, D, nt[4]);
+  }
+}
+
+// Volume moments of the morphology, per material, in double:
+// <w phi_a s_x^2>, <w phi_a s_y^2>, <w phi_a s_z^2>, <w phi_a s_x s_y>,
+// <w phi_a s_x s_z>, <w phi_a s_y s_z>, <w phi_ui> (sums; w = window or 1).
+// With the per-energy constants they give the mean of every tensor entry.
+// Subtracting a constant before the FFT changes only frequency bin 0, which
+// the path always replaces by the mean of its neighbours (src/cudaMain.cu:
+// 123-176); removing it keeps the FP32 FFT's rounding floor proportional to
+// the fluctuations instead of to the (~5x larger) mean.
+constexpr int kMoments = 7;
+struct MomentParams {
+  const float4 *vox;
+  uint32_t nx, ny, nz, nmat;
+  size_t nvox;
+  const float *hann_x, *hann_y, *hann_z;
+  double *out;  // [nmat][kMoments], accumulated
+};
+
+template <int MORPH>
+__global__ void __launch_bounds__(256) k_moments(MomentParams p) {
+  __shared__ double red[8][kMoments];
+  const uint32_t m = blockIdx.y;
+  // per-thread sums in float (a few hundred terms; only an approximate mean is
+  // needed), block and grid reduction in double
+  float acc[kMoments];
+#pragma unroll
+  for (int q = 0; q < kMoments; ++q) acc[q] = 0.f;
+  const size_t stride = size_t(gridDim.x) * blockDim.x;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
+    float sx, sy, sz, pa, pui;
+    director<MORPH>(__ldg(&p.vox[m * p.nvox + i]), sx, sy, sz, pa, pui);
+    float w = 1.f;
+    if (p.hann_x) {
+      const uint32_t x = uint32_t(i % p.nx), y = uint32_t((i / p.nx) % p.ny), z = uint32_t(i / (size_t(p.nx) * p.ny));
+      w = p.hann_x[x] * p.hann_y[y] * p.hann_z[z];
+    }
+    const float wa = w * pa;
+    acc[0] += wa * sx * sx;
+    acc[1] += wa * sy * sy;
+    acc[2] += wa * sz * sz;
+    acc[3] += wa * sx * sy;
+    acc[4] += wa * sx * sz;
+    acc[5] += wa * sy * sz;
+    acc[6] += w * pui;
+  }
+#pragma unroll
+  for (int q = 0; q < kMoments; ++q) {
+    double v = double(acc[q]);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kMoments) {
+    double v = 0.0;
+    for (int wi = 0; wi < int(blockDim.x >> 5); ++wi) v += red[wi][threadIdx.x];
+    atomicAdd(&p.out[m * kMoments + threadIdx.x], v);
+  }
+}
+
+// Mean of each windowed tensor entry for every energy: out[e][6] (xx xy xz yy yz zz).
+__global__ void k_entry_means(const double *__restrict__ mom, uint32_t nmat, size_t nvox,
+                              const MaterialConsts *__restrict__ mcs, uint32_t ne, float2 *__restrict__ out) {
+  for (uint32_t e = threadIdx.x; e < ne; e += blockDim.x) {
+    double r[6][2] = {};
+    for (uint32_t m = 0; m < nmat; ++m) {
+      const double *M = mom + m * kMoments;
+      const MaterialConsts &c = mcs[e];
+      const double A[2] = {c.A[m].x, c.A[m].y}, B[2] = {c.B[m].x, c.B[m].y};
+      const double C[2] = {c.C[m].x, c.C[m].y}, D[2] = {c.D[m].x, c.D[m].y};
+      for (int k = 0; k < 2; ++k) {
+        r[0][k] += A[k] * M[0] + B[k] * (M[1] + M[2]) + C[k] * M[6];
+        r[3][k] += A[k] * M[1] + B[k] * (M[0] + M[2]) + C[k] * M[6];
+        r[5][k] += A[k] * M[2] + B[k] * (M[0] + M[1]) + C[k] * M[6];
+        r[1][k] += D[k] * M[3];
+        r[2][k] += D[k] * M[4];
+        r[4][k] += D[k] * M[5];
+      }
+    }
+    for (int q = 0; q < 6; ++q)
+      out[e * 6 + q] = make_float2(float(r[q][0] / double(nvox)), float(r[q][1] / double(nvox)));
   }
 }
 
@@ -124,23 +220,44 @@ __global__ void __launch_bounds__(256) k_build(BuildParams p, const MaterialCons
       w = p.hann_x[x] * p.hann_y[y] * p.hann_z[z];
     }
     if (p.mode == 0) {
-      for (uint32_t v = 0; v < p.nvol; ++v) p.out[v * p.nvox + i] = cscale(nt[p.entry[v]], w);
+#pragma unroll
+      for (int v = 0; v < 6; ++v) {
+        if (uint32_t(v) < p.nvol) {
+          float2 val = cscale(nt[v], w);
+          if (p.mean) val = csub(val, p.mean[v]);
+          p.out[v * p.nvox + i] = val;
+        }
+      }
     } else {
       // p = Nt E (uniaxial.h:106-151), then R^T p in the MATERIAL frame (:163-165)
       const float e0 = p.E[0], e1 = p.E[1], e2 = p.E[2];
       float2 q[3];
-      q[0] = cadd(cadd(cscale(nt[0], e0), cscale(nt[1], e1)), cscale(nt[2], e2));
-      q[1] = cadd(cadd(cscale(nt[1], e0), cscale(nt[3], e1)), cscale(nt[4], e2));
-      q[2] = cadd(cadd(cscale(nt[2], e0), cscale(nt[4], e1)), cscale(nt[5], e2));
-      if (p.material_frame) {
-        float2 r[3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-          r[a] = cadd(cadd(cscale(q[0], p.Rm[0 * 3 + a]), cscale(q[1], p.Rm[1 * 3 + a])), cscale(q[2], p.Rm[2 * 3 + a]));
-        q[0] = r[0], q[1] = r[1], q[2] = r[2];
+      for (int pass = 0; pass < 2; ++pass) {
+        // pass 0: this voxel; pass 1 (only with means): the mean tensor, same linear map
+        float2 t[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) t[c] = pass == 0 ? cscale(nt[c], w) : (p.mean ? p.mean[c] : make_float2(0.f, 0.f));
+        float2 r3[3];
+        r3[0] = cadd(cadd(cscale(t[0], e0), cscale(t[1], e1)), cscale(t[2], e2));
+        r3[1] = cadd(cadd(cscale(t[1], e0), cscale(t[3], e1)), cscale(t[4], e2));
+        r3[2] = cadd(cadd(cscale(t[2], e0), cscale(t[4], e1)), cscale(t[5], e2));
+        if (p.material_frame) {
+          float2 r[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+            r[a] = cadd(cadd(cscale(r3[0], p.Rm[0 * 3 + a]), cscale(r3[1], p.Rm[1 * 3 + a])), cscale(r3[2], p.Rm[2 * 3 + a]));
+          r3[0] = r[0], r3[1] = r[1], r3[2] = r[2];
+        }
+        if (pass == 0) {
+          q[0] = r3[0], q[1] = r3[1], q[2] = r3[2];
+        } else {
+          q[0] = csub(q[0], r3[0]), q[1] = csub(q[1], r3[1]), q[2] = csub(q[2], r3[2]);
+        }
+        if (!p.mean) break;
       }
 #pragma unroll
-      for (int c = 0; c < 3; ++c) p.out[c * p.nvox + i] = cscale(q[c], w);
+      for (int c = 0; c < 3; ++c) p.out[c * p.nvox + i] = q[c];
     }
   }
 }
@@ -157,7 +274,7 @@ __global__ void __launch_bounds__(256) k_build(BuildParams p, const MaterialCons
 struct FftAxis {
   uint32_t n;            // line length
   uint32_t nstages;
-  uint32_t radix[16];
+  uint64_t radix_code;   // radix of stage s in bits [4s, 4s+4)
   const float2 *tw;      // W_n^m, m in [0, n)
 };
 
@@ -226,45 +343,51 @@ __device__ __forceinline__ void dft_odd(float2 *v) {
   for (int q = 0; q < R; ++q) v[q] = out[q];
 }
 
-// One Stockham stage of radix R over all lines of the block.
+// One Stockham stage of radix R over all lines of the block.  The block holds
+// `nv` groups of `lines` interleaved lines; element i of line l in group v
+// lives at (v * n + i) * S + l.
 template <int R>
 __device__ __forceinline__ void stockham_stage(const float2 *__restrict__ src, float2 *__restrict__ dst, uint32_t n,
-                                               uint32_t ns, uint32_t lines, uint32_t S, const float2 *__restrict__ tw) {
+                                               uint32_t ns, uint32_t lines, uint32_t nv, uint32_t S,
+                                               const float2 *__restrict__ tw) {
   const uint32_t m = n / R;               // butterflies per line
   const uint32_t twstep = n / (ns * R);   // W_{ns R}^{k r} = W_n^{k r twstep}
-  const uint32_t jobs = m * lines;
+  const uint32_t jobs = m * lines * nv;
   for (uint32_t job = threadIdx.x; job < jobs; job += blockDim.x) {
-    const uint32_t l = job % lines, j = job / lines;
+    const uint32_t l = job % lines, rest = job / lines;
+    const uint32_t j = rest % m, v = rest / m;
     const uint32_t k = j % ns;
-    float2 v[R];
+    const size_t vb = size_t(v) * n;
+    float2 w[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = src[(j + r * m) * S + l];
+    for (int r = 0; r < R; ++r) w[r] = src[(vb + j + r * m) * S + l];
     if (ns > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[k * r * twstep]));
+      for (int r = 1; r < R; ++r) w[r] = cmul(w[r], __ldg(&tw[k * r * twstep]));
     }
-    if (R == 2) dft2(v);
-    if (R == 4) dft4(v[0], v[1], v[2], v[3]);
-    if (R == 8) dft8(v);
-    if (R == 3 || R == 5 || R == 7) dft_odd<(R == 2 || R == 4 || R == 8) ? 3 : R>(v);
+    if (R == 2) dft2(w);
+    if (R == 4) dft4(w[0], w[1], w[2], w[3]);
+    if (R == 8) dft8(w);
+    if (R == 3 || R == 5 || R == 7) dft_odd<(R == 2 || R == 4 || R == 8) ? 3 : R>(w);
     const uint32_t base = (j / ns) * ns * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) dst[(base + r * ns) * S + l] = v[r];
+    for (int r = 0; r < R; ++r) dst[(vb + base + r * ns) * S + l] = w[r];
   }
 }
 
 // Runs all stages; returns the buffer holding the result.
-__device__ __forceinline__ float2 *stockham(float2 *a, float2 *b, const FftAxis &ax, uint32_t lines, uint32_t S) {
+__device__ __forceinline__ float2 *stockham(float2 *a, float2 *b, const FftAxis &ax, uint32_t lines, uint32_t S,
+                                            uint32_t nv = 1) {
   uint32_t ns = 1;
   for (uint32_t s = 0; s < ax.nstages; ++s) {
-    const uint32_t R = ax.radix[s];
+    const uint32_t R = uint32_t(ax.radix_code >> (4 * s)) & 15u;
     switch (R) {
-      case 8: stockham_stage<8>(a, b, ax.n, ns, lines, S, ax.tw); break;
-      case 4: stockham_stage<4>(a, b, ax.n, ns, lines, S, ax.tw); break;
-      case 2: stockham_stage<2>(a, b, ax.n, ns, lines, S, ax.tw); break;
-      case 3: stockham_stage<3>(a, b, ax.n, ns, lines, S, ax.tw); break;
-      case 5: stockham_stage<5>(a, b, ax.n, ns, lines, S, ax.tw); break;
-      default: stockham_stage<7>(a, b, ax.n, ns, lines, S, ax.tw); break;
+      case 8: stockham_stage<8>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
+      case 4: stockham_stage<4>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
+      case 2: stockham_stage<2>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
+      case 3: stockham_stage<3>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
+      case 5: stockham_stage<5>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
+      default: stockham_stage<7>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
     }
     __syncthreads();
     float2 *t = a;
@@ -275,8 +398,18 @@ __device__ __forceinline__ float2 *stockham(float2 *a, float2 *b, const FftAxis 
   return a;
 }
 
+// Asynchronous global -> shared copies (cp.async, 8 bytes each): every load of
+// a tile is in flight at once instead of one per thread per loop iteration.
+__device__ __forceinline__ void cp_async8(void *smem_dst, const void *gmem_src) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // AXIS 0: lines along x (rows).  AXIS 1: along y.  AXIS 2: along z.
-// Grid: x = tiles, y = volume.  TX lines per tile.
+// Grid: x = tiles, y = volume.  TX lines per tile (TX * n ~ 4096 elements,
+// two 32 KB buffers, 3 blocks of 512 threads per SM).
+constexpr int kFftThreads = 512;
 struct FftPassParams {
   float2 *data;
   uint32_t nx, ny, nz;
@@ -286,7 +419,7 @@ struct FftPassParams {
 };
 
 template <int AXIS>
-__global__ void __launch_bounds__(256) k_fft_pass(FftPassParams p) {
+__global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
   extern __shared__ float2 smem[];
   const uint32_t n = p.ax.n, TX = p.tx, S = TX + 1;
   float2 *bufa = smem, *bufb = smem + size_t(n) * S;
@@ -317,29 +450,30 @@ __global__ void __launch_bounds__(256) k_fft_pass(FftPassParams p) {
     }
   }
   const uint32_t total = n * TX;
-  if (AXIS == 0) {
-    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
-      const uint32_t l = t / n, i = t % n;
-      bufa[i * S + l] = l < valid ? vol[base + l * lstep + i * estep] : make_float2(0.f, 0.f);
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+    uint32_t l, i;
+    if (AXIS == 0) {
+      l = t / n, i = t % n;  // consecutive threads walk along a row
+    } else {
+      l = t % TX, i = t / TX;  // consecutive threads walk across the tile's columns
     }
-  } else {
-    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
-      const uint32_t l = t % TX, i = t / TX;
-      bufa[i * S + l] = l < valid ? vol[base + l * lstep + i * estep] : make_float2(0.f, 0.f);
-    }
+    float2 *dst = &bufa[i * S + l];
+    if (l < valid)
+      cp_async8(dst, &vol[base + l * lstep + i * estep]);
+    else
+      *dst = make_float2(0.f, 0.f);
   }
+  cp_async_wait_all();
   __syncthreads();
   const float2 *res = stockham(bufa, bufb, p.ax, TX, S);
-  if (AXIS == 0) {
-    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
-      const uint32_t l = t / n, i = t % n;
-      if (l < valid) vol[base + l * lstep + i * estep] = res[i * S + l];
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+    uint32_t l, i;
+    if (AXIS == 0) {
+      l = t / n, i = t % n;
+    } else {
+      l = t % TX, i = t / TX;
     }
-  } else {
-    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
-      const uint32_t l = t % TX, i = t / TX;
-      if (l < valid) vol[base + l * lstep + i * estep] = res[i * S + l];
-    }
+    if (l < valid) vol[base + l * lstep + i * estep] = res[i * S + l];
   }
 }
 
