@@ -151,13 +151,17 @@ def load_traffic(workload):
         return {}
 
 
-def algorithmic_bytes(kernel, w, nvol, nang, ne_step):
-    """Compulsory bytes per launch (each distinct element read once, written once)."""
+def algorithmic_bytes(kernel, w, nvol, nang, planes):
+    """Compulsory bytes per launch (each distinct element read once, written once).
+
+    planes = z planes kept after the fused build + z FFT (nz when not pruned)."""
     V, P, M = w.nvox, w.nx * w.ny, w.num_material
     table = {
         "k_build": (16 * M + 8 * nvol) * V,
-        "k_fft_pass<x>": 2 * 8 * nvol * V,
-        "k_fft_pass<y>": 2 * 8 * nvol * V,
+        "k_build_fft_z": 16 * M * V + 8 * nvol * planes * P,
+        "k_moments": 16 * M * V,
+        "k_fft_pass<x>": 2 * 8 * nvol * planes * P,
+        "k_fft_pass<y>": 2 * 8 * nvol * planes * P,
         "k_fft_pass<z>": 2 * 8 * nvol * V,
         "k_ewald_angles": 2 * 8 * nvol * P + 4 * nang * P,
         "k_rotate_average": 4 * nang * P + 4 * P,
@@ -293,15 +297,16 @@ def main():
     torch.cuda.synchronize()
     kernels, dropped = _native.profile_end()
     launches_per_step = sum(n for n, _ in kernels.values()) / prof_steps
-    nvol = 5
+    info = _native.plan_info(opts)
+    nvol, planes = info["nvol"], info["planes"]
     dom = max(kernels.items(), key=lambda kv: kv[1][1])
     dom_name, (dom_n, dom_ms) = dom
     peak, peak_kind = load_peaks()
-    dom_bytes = algorithmic_bytes(dom_name, w, nvol, nang, len(energies))
+    dom_bytes = algorithmic_bytes(dom_name, w, nvol, nang, planes)
     achieved = dom_bytes / (dom_ms / dom_n / 1000.0) / 1e9
     traffic = load_traffic(w.name).get(dom_name)
     kernel_table = {k: {"launches_per_step": n / prof_steps, "ms_per_launch": ms / n,
-                        "gbs": (algorithmic_bytes(k, w, nvol, nang, len(energies)) or 0) / (ms / n / 1000.0) / 1e9}
+                        "gbs": (algorithmic_bytes(k, w, nvol, nang, planes) or 0) / (ms / n / 1000.0) / 1e9}
                     for k, (n, ms) in kernels.items()}
 
     result = {
@@ -322,6 +327,7 @@ def main():
                      "algorithmic_bytes_per_launch": dom_bytes},
         "kernels": kernel_table,
         "gpu_launches": int(round(launches_per_step * args.steps)),
+        "plan": info,
         "clocks": None,
     }
     if rank == 0:

@@ -79,6 +79,8 @@ def lib():
                                    ctypes.c_uint32, ctypes.c_void_p]
     L.cyr_warp_affine_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+    L.cyr_plan_info.argtypes = [opt_p, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32]
+    L.cyr_device_errors.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
     L.cyr_profile_begin.argtypes = [ctypes.c_uint32]
     L.cyr_profile_end.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
                                   ctypes.POINTER(ctypes.c_uint32)]
@@ -182,6 +184,19 @@ def warp_affine_device(d_src: int, d_dst: int, width: int, height: int, coeffs, 
     c = np.ascontiguousarray(np.asarray(coeffs, np.float64).reshape(6))
     check(lib().cyr_warp_affine_device(ctypes.c_void_p(d_src), ctypes.c_void_p(d_dst), width, height,
                                        c.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_void_p(stream)))
+
+
+def plan_info(opts: Options) -> dict:
+    info = (ctypes.c_uint32 * 6)()
+    check(lib().cyr_plan_info(opts.ref, info, 6))
+    return {"nvol": info[0], "planes": info[1], "zlo": info[2], "pruned": bool(info[3]), "angles": info[4],
+            "k": info[5]}
+
+
+def device_errors() -> int:
+    n = ctypes.c_uint32(0)
+    check(lib().cyr_device_errors(ctypes.byref(n)))
+    return int(n.value)
 
 
 def profile_begin(max_launches: int = 65536) -> None:

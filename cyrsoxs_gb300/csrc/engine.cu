@@ -121,10 +121,10 @@ struct DeviceBuffer {
 
 // Optional per-launch timing: an event pair around every kernel launch,
 // read back after the caller has synchronised (cyr_profile_end).
-enum Stage { kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kNumStages };
+enum Stage { kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kBuildZ, kNumStages };
 const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_pass<y>", "k_fft_pass<z>", "k_dc",
                                              "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp",
-                                             "k_moments", "k_entry_means"};
+                                             "k_moments", "k_entry_means", "k_build_fft_z"};
 
 struct Profiler {
   bool active = false;
@@ -153,7 +153,7 @@ struct DeviceContext {
   std::mutex mu;
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
-  DeviceBuffer spec, images, avg, params, dc, vox_in, out_in, moments, means;
+  DeviceBuffer spec, images, avg, params, dc, vox_in, out_in, moments, means, errors, conv, flags;
   cudaEvent_t last_use = nullptr;  // completion of the last request that used the scratch
 };
 
@@ -184,6 +184,8 @@ int setup_attrs(DeviceContext &ctx) {
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaEventCreateWithFlags(&ctx.last_use, cudaEventDisableTiming));
   ctx.attrs_done = true;
   return CYR_OK;
@@ -212,6 +214,9 @@ int make_axis(DeviceContext &ctx, uint32_t n, FftAxis &ax) {
   std::vector<uint32_t> r;
   if (!factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u has a prime factor above 7", n);
   ax.n = n;
+  ax.log2n = 0;
+  if ((n & (n - 1)) == 0 && n > 1)
+    while ((1u << ax.log2n) < n) ++ax.log2n;
   ax.nstages = uint32_t(r.size());
   ax.radix_code = 0;
   for (size_t i = 0; i < r.size(); ++i) ax.radix_code |= uint64_t(r[i]) << (4 * i);
@@ -219,10 +224,11 @@ int make_axis(DeviceContext &ctx, uint32_t n, FftAxis &ax) {
 }
 
 // In-place forward 3D FFT of `count` volumes.
-int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st) {
+int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
+          bool skip_z = false) {
   const size_t nvox = size_t(nx) * ny * nz;
   const uint32_t dims[3] = {nx, ny, nz};
-  for (int axis = 0; axis < 3; ++axis) {
+  for (int axis = 0; axis < (skip_z ? 2 : 3); ++axis) {
     const uint32_t n = dims[axis];
     if (n == 1) continue;
     FftPassParams p{};
@@ -257,7 +263,7 @@ int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t n
 struct Plan {
   uint32_t nx, ny, nz, nmat, ne, nk, nang;
   size_t nvox, npix;
-  bool material_frame, hanning, twod;
+  bool material_frame, hanning, twod, interp_nn = false, euler = false;
   uint32_t nbasis, nvol;           // LAB: 2 or 3 bases; MATERIAL: 1 basis, 3 volumes
   std::vector<KFrame> frames;
   Mat3f detector;
@@ -270,7 +276,65 @@ struct Plan {
   std::vector<Mat3f> rmats;             // [k][angle] (MATERIAL frame)
   std::vector<float> eangles;           // [k][angle]
   float start, inc;
+  // z pruning: the spectra keep shifted planes [zlo, zlo + kz) only
+  bool pruned = false;
+  uint32_t zlo = 0, kz = 0, ztx = 1;
+  size_t vstride = 0;                   // elements per spectrum volume
+  uint32_t p0 = 0, p1 = 0, pn = 0;      // planes of unshifted z bins 0, 1, nz-1
 };
+
+inline uint32_t igor_host(uint32_t j, uint32_t n) { return j <= n / 2 ? n / 2 - j : n + n / 2 - j; }
+
+// Shifted z planes the Ewald projection can read, for every energy and k of
+// the request.  posz = -kz + sqrt(val) grows with val = k^2 - (kx+qx)^2 -
+// (ky+qy)^2, which separates in X and Y, so the extremes over the detector
+// come from the extremes of two 1D arrays; val >= 0 bounds posz below by -kz.
+// The range is widened by a plane on each side and always holds the planes
+// of the DC neighbours.
+void kept_planes(const cyr_options *o, Plan &pl) {
+  const float start = -static_cast<float>(kPi / o->phys_size);
+  const float dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nx - 1) * 1.0));
+  const float dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.ny - 1) * 1.0));
+  const float dz = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nz - 1) * 1.0));
+  double tlo = 1e300, thi = -1e300;
+  for (uint32_t e = 0; e < pl.ne; ++e) {
+    const float kmag = static_cast<float>(2 * kPi / static_cast<float>(1239.84197 / o->energies[e]));
+    for (const KFrame &f : pl.frames) {
+      const double kx = kmag * f.k.x, ky = kmag * f.k.y, kz = kmag * f.k.z;
+      double amin = 1e300, bmin = 1e300;
+      for (uint32_t X = 0; X + 1 < pl.nx; ++X) {
+        const double a = kx + double(start + X * dx);
+        amin = std::min(amin, a * a);
+      }
+      for (uint32_t Y = 0; Y + 1 < pl.ny; ++Y) {
+        const double b = ky + double(start + Y * dy);
+        bmin = std::min(bmin, b * b);
+      }
+      const double vmax = double(kmag) * kmag - amin - bmin;
+      if (vmax < 0) continue;
+      tlo = std::min(tlo, (-kz - start) / dz);
+      thi = std::max(thi, (-kz + std::sqrt(vmax) - start) / dz);
+    }
+  }
+  long lo = long(pl.nz), hi = -1;
+  if (tlo <= thi) {
+    if (pl.interp_nn) {
+      lo = long(std::floor(tlo + 0.5)) - 1, hi = long(std::floor(thi + 0.5)) + 1;
+    } else {
+      lo = long(std::floor(tlo)) - 1, hi = long(std::floor(thi)) + 2;
+    }
+    lo = std::max(lo, 0L), hi = std::min(hi, long(pl.nz) - 1);
+  }
+  for (uint32_t u : {0u, 1u, pl.nz - 1}) {
+    const long z = long(igor_host(u % pl.nz, pl.nz));
+    lo = std::min(lo, z), hi = std::max(hi, z);
+  }
+  pl.zlo = uint32_t(lo);
+  pl.kz = uint32_t(hi - lo + 1);
+  pl.p0 = igor_host(0, pl.nz) - pl.zlo;
+  pl.p1 = igor_host(1 % pl.nz, pl.nz) - pl.zlo;
+  pl.pn = igor_host(pl.nz - 1, pl.nz) - pl.zlo;
+}
 
 template <class T>
 size_t arena_put(std::vector<unsigned char> &a, const T *src, size_t count) {
@@ -358,6 +422,21 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
     pl.nbasis = any_ez ? 3 : 2;
     pl.nvol = any_ez ? 6 : 5;
   }
+  pl.interp_nn = o->ewald_interpolation == 0;
+  pl.euler = o->morphology_type == 0;
+  pl.vstride = pl.nvox;
+  pl.p0 = 0, pl.p1 = 1 % pl.nz, pl.pn = pl.nz - 1;
+  if (!pl.twod) {
+    // fused build + z FFT: lines per block so that two 512-thread blocks fit an SM
+    uint32_t tx = 16;
+    while (tx > 1 && size_t(2) * pl.nvol * pl.nz * (tx + 1) * sizeof(float2) > 104 * 1024) tx /= 2;
+    if (size_t(2) * pl.nvol * pl.nz * (tx + 1) * sizeof(float2) <= kFftSmemBudget) {
+      pl.pruned = true;
+      pl.ztx = tx;
+      kept_planes(o, pl);
+      pl.vstride = size_t(pl.kz) * pl.npix;
+    }
+  }
   // material constants per energy, in double, scaled by 1/4pi (uniaxial.h:155-162)
   std::vector<MaterialConsts> mcs(pl.ne);
   const double s = 1.0 / (4.0 * kPi);
@@ -431,7 +510,7 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
 }
 
 size_t request_bytes(const Plan &pl) {
-  return pl.nvol * pl.nvox * sizeof(float2) + size_t(pl.nang) * pl.npix * sizeof(float) + pl.npix * sizeof(float) +
+  return pl.nvol * pl.vstride * sizeof(float2) + (pl.euler ? pl.nvox * pl.nmat * sizeof(float4) : 0) + size_t(pl.nang) * pl.npix * sizeof(float) + pl.npix * sizeof(float) +
          pl.arena.size() + 64 * sizeof(float2);
 }
 
@@ -442,7 +521,10 @@ EwaldParams ewald_params(const Plan &pl, const cyr_options *o, const unsigned ch
   p.spec = spec;
   p.dc = dc;
   p.nx = pl.nx, p.ny = pl.ny, p.nz = pl.nz;
-  p.nvox = pl.nvox;
+  p.nvox = pl.vstride;
+  p.zshifted = pl.pruned ? 1u : 0u;
+  p.zlo = pl.zlo;
+  p.nplanes = pl.kz;
   p.nbasis = pl.nbasis;
   if (pl.material_frame) {
     for (int c = 0; c < 3; ++c) p.vol[c][0] = c;
@@ -472,7 +554,9 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   CYR_TRY(setup_attrs(ctx));
   // scratch (grow-only); wait for the previous user of the scratch
   CYR_CUDA(cudaStreamWaitEvent(st, ctx.last_use, 0));
-  CYR_TRY(ctx.spec.ensure(pl.nvol * pl.nvox * sizeof(float2)));
+  CYR_TRY(ctx.spec.ensure(pl.nvol * pl.vstride * sizeof(float2)));
+  CYR_TRY(ctx.errors.ensure(sizeof(unsigned)));
+  CYR_CUDA(cudaMemsetAsync(ctx.errors.ptr, 0, sizeof(unsigned), st));
   CYR_TRY(ctx.images.ensure(size_t(pl.nang) * pl.npix * sizeof(float)));
   CYR_TRY(ctx.avg.ensure(pl.npix * sizeof(float)));
   CYR_TRY(ctx.dc.ensure(8 * sizeof(float2)));
@@ -483,6 +567,11 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   CYR_TRY(ctx.moments.ensure(size_t(pl.nmat) * kMoments * sizeof(double)));
   CYR_TRY(ctx.means.ensure(size_t(pl.ne) * 6 * sizeof(float2)));
   CYR_CUDA(cudaMemsetAsync(ctx.moments.ptr, 0, size_t(pl.nmat) * kMoments * sizeof(double), st));
+  // Euler morphologies are converted once per request to the trigonometry-free vector form
+  const bool convert = o->morphology_type == 0;
+  CYR_TRY(ctx.flags.ensure(sizeof(unsigned)));
+  CYR_CUDA(cudaMemsetAsync(ctx.flags.ptr, 0, sizeof(unsigned), st));
+  if (convert) CYR_TRY(ctx.conv.ensure(pl.nvox * pl.nmat * sizeof(float4)));
   {
     MomentParams mp{};
     mp.vox = d_vox;
@@ -494,6 +583,8 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       mp.hann_z = reinterpret_cast<const float *>(dp + pl.off_hz);
     }
     mp.out = ctx.moments.as<double>();
+    mp.conv = convert ? ctx.conv.as<float4>() : nullptr;
+    mp.neg = ctx.flags.as<unsigned>();
     int nsm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx.device));
     const dim3 grid(uint32_t(std::max<size_t>(1, std::min<size_t>((pl.nvox + 255) / 256, size_t(nsm) * 8))), pl.nmat);
@@ -523,6 +614,8 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   bp.nvox = pl.nvox;
   bp.morphology = o->morphology_type;
   bp.out = spec;
+  bp.conv = convert ? ctx.conv.as<float4>() : nullptr;
+  bp.neg = ctx.flags.as<unsigned>();
   if (pl.hanning) {
     bp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
     bp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
@@ -532,6 +625,47 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
   const uint32_t build_blocks = uint32_t(std::min<size_t>((pl.nvox + 255) / 256, size_t(sms) * 8));
   EwaldParams ep = ewald_params(pl, o, dp, spec, dc, images);
+  ep.errors = ctx.errors.as<unsigned>();
+  FftAxis az{};
+  if (pl.pruned) CYR_TRY(make_axis(ctx, pl.nz, az));
+  // spectra of the current BuildParams (nvol volumes): pruned (build + z FFT
+  // fused, then x and y on the kept planes) or full (build, then 3 passes)
+  auto spectra = [&](const MaterialConsts *mce) -> int {
+    int slot;
+    if (pl.pruned) {
+      BuildZParams zp{};
+      zp.b = bp;
+      zp.az = az;
+      zp.tx = pl.ztx;
+      zp.zlo = pl.zlo;
+      zp.kz = pl.kz;
+      zp.out = spec;
+      const size_t smem = size_t(2) * bp.nvol * pl.nz * (pl.ztx + 1) * sizeof(float2);
+      const dim3 grid((pl.nx + pl.ztx - 1) / pl.ztx * pl.ny);
+      slot = ctx.prof.begin(kBuildZ, st);
+      if (o->morphology_type == 0)
+        k_build_fft_z<0><<<grid, kFftThreads, smem, st>>>(zp, mce);
+      else
+        k_build_fft_z<1><<<grid, kFftThreads, smem, st>>>(zp, mce);
+      ctx.prof.end(slot, st);
+      CYR_CUDA(cudaGetLastError());
+      CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.kz, bp.nvol, st, true));
+    } else {
+      slot = ctx.prof.begin(kBuild, st);
+      if (o->morphology_type == 0)
+        k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
+      else
+        k_build<1><<<build_blocks, 256, 0, st>>>(bp, mce);
+      ctx.prof.end(slot, st);
+      CYR_CUDA(cudaGetLastError());
+      CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, bp.nvol, st));
+    }
+    slot = ctx.prof.begin(kDc, st);
+    k_dc<<<1, 32, 0, st>>>(spec, bp.nvol, pl.vstride, pl.nx, pl.ny, pl.nz, pl.p0, pl.p1, pl.pn, dc);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+    return CYR_OK;
+  };
   const unsigned pix_blocks = unsigned((pl.npix + 255) / 256);
   const int W = int(pl.ny), H = int(pl.nx);  // the reference hands NPP width = Ny, height = Nx
   const WarpCoef *dwarp = reinterpret_cast<const WarpCoef *>(dp + pl.off_warp);
@@ -548,18 +682,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       bp.mode = 0;
       bp.nvol = pl.nvol;
       bp.mean = ctx.means.as<float2>() + size_t(e) * 6;
-      int slot = ctx.prof.begin(kBuild, st);
-      if (o->morphology_type == 0)
-        k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
-      else
-        k_build<1><<<build_blocks, 256, 0, st>>>(bp, mce);
-      ctx.prof.end(slot, st);
-      CYR_CUDA(cudaGetLastError());
-      CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, pl.nvol, st));
-      slot = ctx.prof.begin(kDc, st);
-      k_dc<<<1, 32, 0, st>>>(spec, pl.nvol, pl.nvox, pl.nx, pl.ny, pl.nz, dc);
-      ctx.prof.end(slot, st);
-      CYR_CUDA(cudaGetLastError());
+      CYR_TRY(spectra(mce));
     }
     for (uint32_t k = 0; k < pl.nk; ++k) {
       const KFrame &f = pl.frames[k];
@@ -583,21 +706,11 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
           bp.mean = ctx.means.as<float2>() + size_t(e) * 6;
           for (int c = 0; c < 3; ++c) bp.E[c] = pl.evec[ka * 3 + c];
           std::memcpy(bp.Rm, pl.rmats[ka].m, sizeof bp.Rm);
-          int slot = ctx.prof.begin(kBuild, st);
-          if (o->morphology_type == 0)
-            k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
-          else
-            k_build<1><<<build_blocks, 256, 0, st>>>(bp, mce);
-          ctx.prof.end(slot, st);
-          CYR_CUDA(cudaGetLastError());
-          CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, 3, st));
-          slot = ctx.prof.begin(kDc, st);
-          k_dc<<<1, 32, 0, st>>>(spec, 3, pl.nvox, pl.nx, pl.ny, pl.nz, dc);
-          ctx.prof.end(slot, st);
+          CYR_TRY(spectra(mce));
           ep.nangles = 1;
           ep.coef = dcoef + ka;  // nbasis == 1, coefficient 1
           ep.images = images + size_t(a) * pl.npix;
-          slot = ctx.prof.begin(kEwald, st);
+          const int slot = ctx.prof.begin(kEwald, st);
           k_ewald_angles<<<pix_blocks, 256, 0, st>>>(ep);
           ctx.prof.end(slot, st);
           CYR_CUDA(cudaGetLastError());
@@ -661,6 +774,31 @@ int cyr_required_device_bytes(const cyr_options *opt, size_t *bytes) {
   return CYR_OK;
 }
 
+int cyr_plan_info(const cyr_options *opt, uint32_t *info, uint32_t n) {
+  if (!info) return fail(CYR_ERR_ARGUMENT, "info pointer is null");
+  CYR_TRY(validate(opt));
+  std::vector<float> dummy(size_t(opt->num_energies) * opt->num_material * 4, 0.f);
+  Plan pl;
+  CYR_TRY(make_plan(opt, dummy.data(), pl));
+  const uint32_t v[6] = {pl.nvol, pl.pruned ? pl.kz : pl.nz, pl.zlo, pl.pruned ? 1u : 0u, pl.nang, pl.nk};
+  for (uint32_t i = 0; i < n && i < 6; ++i) info[i] = v[i];
+  return CYR_OK;
+}
+
+int cyr_device_errors(uint32_t *count) {
+  if (!count) return fail(CYR_ERR_ARGUMENT, "count pointer is null");
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  *count = 0;
+  if (!ctx->errors.ptr) return CYR_OK;
+  CYR_CUDA(cudaDeviceSynchronize());
+  unsigned h = 0;
+  CYR_CUDA(cudaMemcpy(&h, ctx->errors.ptr, sizeof h, cudaMemcpyDeviceToHost));
+  *count = h;
+  return CYR_OK;
+}
+
 int cyr_release_scratch(void) {
   DeviceContext *ctx = nullptr;
   CYR_TRY(get_context(&ctx));
@@ -673,6 +811,9 @@ int cyr_release_scratch(void) {
   ctx->dc.release();
   ctx->moments.release();
   ctx->means.release();
+  ctx->errors.release();
+  ctx->conv.release();
+  ctx->flags.release();
   ctx->vox_in.release();
   ctx->out_in.release();
   return CYR_OK;
@@ -718,7 +859,13 @@ static int cuda_main_impl(const cyr_options *opt, const float *optical, const fl
       break;
     }
     const cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) rc = fail(CYR_ERR_CUDA, "simulation failed: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "simulation failed: %s", cudaGetErrorString(e));
+      break;
+    }
+    unsigned errs = 0;
+    if (cudaMemcpy(&errs, ctx->errors.ptr, sizeof errs, cudaMemcpyDeviceToHost) == cudaSuccess && errs != 0)
+      rc = fail(CYR_ERR_CUDA, "%u detector pixels needed z planes outside the kept range", errs);
   } while (false);
   cudaStreamDestroy(st);
   return rc;

@@ -57,6 +57,8 @@ struct BuildParams {
   uint32_t mode;        // 0: tensor entries; 1: p = R-frame polarization
   uint32_t nvol;        // mode 0: entries xx xy xz yy yz [zz] written in this order
   const float2 *mean;   // [6] volume mean of each windowed entry (null: none subtracted)
+  const float4 *conv;   // Euler morphology converted to (sqrt(phi_a) s, phi_ui) per material, or null
+  const unsigned *neg;  // set when some phi_a < 0 (the conversion is then not used)
   float E[3];           // mode 1: E = R x
   float Rm[9];          // mode 1: R (row major), for the MATERIAL frame
   uint32_t material_frame;
@@ -83,21 +85,25 @@ __device__ __forceinline__ void director(float4 s, float &sx, float &sy, float &
   }
 }
 
-template <int MORPH>
+// Tensor entries of one voxel.  With CONV the morphology has been converted
+// to the vector form u = sqrt(phi_a) s, phi_ui (phi_a s_i s_j = u_i u_j),
+// which needs no trigonometry per energy.
+template <int MORPH, bool CONV>
 __device__ __forceinline__ void nt_entries(const BuildParams &p, const MaterialConsts &mc, size_t i, float2 nt[6]) {
 #pragma unroll
   for (int q = 0; q < 6; ++q) nt[q] = make_float2(0.f, 0.f);
+  const float4 *src = CONV ? p.conv : p.vox;
   for (uint32_t m0 = 0; m0 < p.nmat; m0 += 4) {
     float4 sv[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u)  // issue the loads of up to 4 materials before using them
-      if (m0 + u < p.nmat) sv[u] = __ldg(&p.vox[(m0 + u) * p.nvox + i]);
+      if (m0 + u < p.nmat) sv[u] = __ldg(&src[(m0 + u) * p.nvox + i]);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (m0 + u >= p.nmat) break;
       const uint32_t m = m0 + u;
       float sx, sy, sz, pa, pui;
-      director<MORPH>(sv[u], sx, sy, sz, pa, pui);
+      director<CONV ? 1 : MORPH>(sv[u], sx, sy, sz, pa, pui);
       const float xx = sx * sx, yy = sy * sy, zz = sz * sz;
       const float2 A = mc.A[m], B = mc.B[m], C = mc.C[m], D = mc.D[m];
       // diagonal: phi_a (A s_i^2 + B (|s|^2 - s_i^2)) + phi_ui C, with |s|^2 - s_i^2 as the reference sums it
@@ -131,7 +137,9 @@ struct MomentParams {
   uint32_t nx, ny, nz, nmat;
   size_t nvox;
   const float *hann_x, *hann_y, *hann_z;
-  double *out;  // [nmat][kMoments], accumulated
+  double *out;      // [nmat][kMoments], accumulated
+  float4 *conv;     // Euler only: (sqrt(phi_a) s, phi_ui) per material and voxel, or null
+  unsigned *neg;    // set when some phi_a < 0
 };
 
 template <int MORPH>
@@ -147,6 +155,11 @@ __global__ void __launch_bounds__(256) k_moments(MomentParams p) {
   for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
     float sx, sy, sz, pa, pui;
     director<MORPH>(__ldg(&p.vox[m * p.nvox + i]), sx, sy, sz, pa, pui);
+    if (MORPH == 0 && p.conv) {
+      if (pa < 0.f) atomicOr(p.neg, 1u);
+      const float r = sqrtf(fmaxf(pa, 0.f));
+      p.conv[m * p.nvox + i] = make_float4(r * sx, r * sy, r * sz, pui);
+    }
     float w = 1.f;
     if (p.hann_x) {
       const uint32_t x = uint32_t(i % p.nx), y = uint32_t((i / p.nx) % p.ny), z = uint32_t(i / (size_t(p.nx) * p.ny));
@@ -199,66 +212,77 @@ __global__ void k_entry_means(const double *__restrict__ mom, uint32_t nmat, siz
   }
 }
 
+// The values one voxel contributes to the FFT input: mode 0 the windowed tensor
+// entries xx xy xz yy yz [zz] (nvol of them), mode 1 the polarization
+// p = Nt E (uniaxial.h:106-151), rotated by R^T in the MATERIAL frame
+// (:163-165); the volume mean is subtracted when p.mean is set.
+template <int MORPH, bool CONV>
+__device__ __forceinline__ void voxel_values(const BuildParams &p, const MaterialConsts &mc, size_t i, uint32_t x,
+                                             uint32_t y, uint32_t z, float2 out[6]) {
+  float2 nt[6];
+  nt_entries<MORPH, CONV>(p, mc, i, nt);
+  const float w = p.hann_x ? p.hann_x[x] * p.hann_y[y] * p.hann_z[z] : 1.f;
+  if (p.mode == 0) {
+#pragma unroll
+    for (int v = 0; v < 6; ++v) {
+      out[v] = cscale(nt[v], w);
+      if (p.mean) out[v] = csub(out[v], p.mean[v]);
+    }
+    return;
+  }
+  const float e0 = p.E[0], e1 = p.E[1], e2 = p.E[2];
+  float2 q[3];
+#pragma unroll
+  for (int pass = 0; pass < 2; ++pass) {
+    // pass 0: this voxel; pass 1 (only with means): the mean tensor, same linear map
+    float2 t[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) t[c] = pass == 0 ? cscale(nt[c], w) : (p.mean ? p.mean[c] : make_float2(0.f, 0.f));
+    float2 r3[3];
+    r3[0] = cadd(cadd(cscale(t[0], e0), cscale(t[1], e1)), cscale(t[2], e2));
+    r3[1] = cadd(cadd(cscale(t[1], e0), cscale(t[3], e1)), cscale(t[4], e2));
+    r3[2] = cadd(cadd(cscale(t[2], e0), cscale(t[4], e1)), cscale(t[5], e2));
+    if (p.material_frame) {
+      float2 r[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        r[a] = cadd(cadd(cscale(r3[0], p.Rm[0 * 3 + a]), cscale(r3[1], p.Rm[1 * 3 + a])), cscale(r3[2], p.Rm[2 * 3 + a]));
+      r3[0] = r[0], r3[1] = r[1], r3[2] = r[2];
+    }
+    if (pass == 0) {
+      q[0] = r3[0], q[1] = r3[1], q[2] = r3[2];
+    } else {
+      q[0] = csub(q[0], r3[0]), q[1] = csub(q[1], r3[1]), q[2] = csub(q[2], r3[2]);
+    }
+    if (!p.mean) break;
+  }
+  out[0] = q[0], out[1] = q[1], out[2] = q[2];
+  out[3] = out[4] = out[5] = make_float2(0.f, 0.f);
+}
+
+__device__ __forceinline__ void load_consts(MaterialConsts &dst, const MaterialConsts *src) {
+  const float *s = reinterpret_cast<const float *>(src);
+  float *d = reinterpret_cast<float *>(&dst);
+  for (int t = threadIdx.x; t < int(sizeof(MaterialConsts) / 4); t += blockDim.x) d[t] = s[t];
+}
+
 template <int MORPH>
 __global__ void __launch_bounds__(256) k_build(BuildParams p, const MaterialConsts *__restrict__ mcp) {
   __shared__ MaterialConsts mc;
-  {
-    const float *src = reinterpret_cast<const float *>(mcp);
-    float *dst = reinterpret_cast<float *>(&mc);
-    for (int t = threadIdx.x; t < int(sizeof(MaterialConsts) / 4); t += blockDim.x) dst[t] = src[t];
-  }
+  load_consts(mc, mcp);
   __syncthreads();
+  const bool use_conv = MORPH == 0 && p.conv && *p.neg == 0u;
   const size_t stride = size_t(gridDim.x) * blockDim.x;
   for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
-    float2 nt[6];
-    nt_entries<MORPH>(p, mc, i, nt);
-    float w = 1.f;
-    if (p.hann_x) {
-      const uint32_t x = uint32_t(i % p.nx);
-      const uint32_t y = uint32_t((i / p.nx) % p.ny);
-      const uint32_t z = uint32_t(i / (size_t(p.nx) * p.ny));
-      w = p.hann_x[x] * p.hann_y[y] * p.hann_z[z];
-    }
-    if (p.mode == 0) {
+    const uint32_t x = uint32_t(i % p.nx), y = uint32_t((i / p.nx) % p.ny), z = uint32_t(i / (size_t(p.nx) * p.ny));
+    float2 v[6];
+    if (use_conv)
+      voxel_values<MORPH, true>(p, mc, i, x, y, z, v);
+    else
+      voxel_values<MORPH, false>(p, mc, i, x, y, z, v);
 #pragma unroll
-      for (int v = 0; v < 6; ++v) {
-        if (uint32_t(v) < p.nvol) {
-          float2 val = cscale(nt[v], w);
-          if (p.mean) val = csub(val, p.mean[v]);
-          p.out[v * p.nvox + i] = val;
-        }
-      }
-    } else {
-      // p = Nt E (uniaxial.h:106-151), then R^T p in the MATERIAL frame (:163-165)
-      const float e0 = p.E[0], e1 = p.E[1], e2 = p.E[2];
-      float2 q[3];
-#pragma unroll
-      for (int pass = 0; pass < 2; ++pass) {
-        // pass 0: this voxel; pass 1 (only with means): the mean tensor, same linear map
-        float2 t[6];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) t[c] = pass == 0 ? cscale(nt[c], w) : (p.mean ? p.mean[c] : make_float2(0.f, 0.f));
-        float2 r3[3];
-        r3[0] = cadd(cadd(cscale(t[0], e0), cscale(t[1], e1)), cscale(t[2], e2));
-        r3[1] = cadd(cadd(cscale(t[1], e0), cscale(t[3], e1)), cscale(t[4], e2));
-        r3[2] = cadd(cadd(cscale(t[2], e0), cscale(t[4], e1)), cscale(t[5], e2));
-        if (p.material_frame) {
-          float2 r[3];
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-            r[a] = cadd(cadd(cscale(r3[0], p.Rm[0 * 3 + a]), cscale(r3[1], p.Rm[1 * 3 + a])), cscale(r3[2], p.Rm[2 * 3 + a]));
-          r3[0] = r[0], r3[1] = r[1], r3[2] = r[2];
-        }
-        if (pass == 0) {
-          q[0] = r3[0], q[1] = r3[1], q[2] = r3[2];
-        } else {
-          q[0] = csub(q[0], r3[0]), q[1] = csub(q[1], r3[1]), q[2] = csub(q[2], r3[2]);
-        }
-        if (!p.mean) break;
-      }
-#pragma unroll
-      for (int c = 0; c < 3; ++c) p.out[c * p.nvox + i] = q[c];
-    }
+    for (int c = 0; c < 6; ++c)
+      if (uint32_t(c) < p.nvol) p.out[c * p.nvox + i] = v[c];
   }
 }
 
@@ -273,6 +297,7 @@ __global__ void __launch_bounds__(256) k_build(BuildParams p, const MaterialCons
 // ---------------------------------------------------------------------------
 struct FftAxis {
   uint32_t n;            // line length
+  uint32_t log2n;        // log2(n) when n is a power of two, else 0
   uint32_t nstages;
   uint64_t radix_code;   // radix of stage s in bits [4s, 4s+4)
   const float2 *tw;      // W_n^m, m in [0, n)
@@ -349,14 +374,19 @@ __device__ __forceinline__ void dft_odd(float2 *v) {
 template <int R>
 __device__ __forceinline__ void stockham_stage(const float2 *__restrict__ src, float2 *__restrict__ dst, uint32_t n,
                                                uint32_t ns, uint32_t lines, uint32_t nv, uint32_t S,
-                                               const float2 *__restrict__ tw) {
+                                               const float2 *__restrict__ tw, bool pow2, uint32_t lg_lines,
+                                               uint32_t lg_m, uint32_t lg_ns) {
   const uint32_t m = n / R;               // butterflies per line
   const uint32_t twstep = n / (ns * R);   // W_{ns R}^{k r} = W_n^{k r twstep}
   const uint32_t jobs = m * lines * nv;
   for (uint32_t job = threadIdx.x; job < jobs; job += blockDim.x) {
-    const uint32_t l = job % lines, rest = job / lines;
-    const uint32_t j = rest % m, v = rest / m;
-    const uint32_t k = j % ns;
+    const uint32_t l = job & (lines - 1), rest = job >> lg_lines;  // lines is a power of two
+    uint32_t j, v, k, q;
+    if (pow2) {
+      j = rest & (m - 1), v = rest >> lg_m, k = j & (ns - 1), q = j >> lg_ns;
+    } else {
+      j = rest % m, v = rest / m, k = j % ns, q = j / ns;
+    }
     const size_t vb = size_t(v) * n;
     float2 w[R];
 #pragma unroll
@@ -369,31 +399,37 @@ __device__ __forceinline__ void stockham_stage(const float2 *__restrict__ src, f
     if (R == 4) dft4(w[0], w[1], w[2], w[3]);
     if (R == 8) dft8(w);
     if (R == 3 || R == 5 || R == 7) dft_odd<(R == 2 || R == 4 || R == 8) ? 3 : R>(w);
-    const uint32_t base = (j / ns) * ns * R + k;
+    const uint32_t base = q * ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) dst[(vb + base + r * ns) * S + l] = w[r];
   }
 }
 
-// Runs all stages; returns the buffer holding the result.
+// Runs all stages; returns the buffer holding the result.  `lines` must be a
+// power of two.
 __device__ __forceinline__ float2 *stockham(float2 *a, float2 *b, const FftAxis &ax, uint32_t lines, uint32_t S,
                                             uint32_t nv = 1) {
-  uint32_t ns = 1;
+  const bool pow2 = ax.log2n != 0;
+  const uint32_t lg_lines = 31 - __clz(lines);
+  uint32_t ns = 1, lg_ns = 0;
   for (uint32_t s = 0; s < ax.nstages; ++s) {
     const uint32_t R = uint32_t(ax.radix_code >> (4 * s)) & 15u;
+    const uint32_t lg_r = R == 8 ? 3 : R == 4 ? 2 : 1;
+    const uint32_t lg_m = pow2 ? ax.log2n - lg_r : 0;
     switch (R) {
-      case 8: stockham_stage<8>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
-      case 4: stockham_stage<4>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
-      case 2: stockham_stage<2>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
-      case 3: stockham_stage<3>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
-      case 5: stockham_stage<5>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
-      default: stockham_stage<7>(a, b, ax.n, ns, lines, nv, S, ax.tw); break;
+      case 8: stockham_stage<8>(a, b, ax.n, ns, lines, nv, S, ax.tw, pow2, lg_lines, lg_m, lg_ns); break;
+      case 4: stockham_stage<4>(a, b, ax.n, ns, lines, nv, S, ax.tw, pow2, lg_lines, lg_m, lg_ns); break;
+      case 2: stockham_stage<2>(a, b, ax.n, ns, lines, nv, S, ax.tw, pow2, lg_lines, lg_m, lg_ns); break;
+      case 3: stockham_stage<3>(a, b, ax.n, ns, lines, nv, S, ax.tw, false, lg_lines, 0, 0); break;
+      case 5: stockham_stage<5>(a, b, ax.n, ns, lines, nv, S, ax.tw, false, lg_lines, 0, 0); break;
+      default: stockham_stage<7>(a, b, ax.n, ns, lines, nv, S, ax.tw, false, lg_lines, 0, 0); break;
     }
     __syncthreads();
     float2 *t = a;
     a = b;
     b = t;
     ns *= R;
+    lg_ns += lg_r;
   }
   return a;
 }
@@ -477,26 +513,91 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
   }
 }
 
+// Tensor build fused with the z-axis FFT, keeping only the z planes the Ewald
+// projection can read.  A block owns TX consecutive x columns at one y, over
+// all z: it computes the nvol entry volumes for those columns into shared
+// memory, transforms them along z, and writes planes [zlo, zlo + kz) of the
+// SHIFTED z axis (plane zlo + q holds unshifted bin igor(zlo + q)) as
+// out[v][q][y][x].  The x and y FFTs then run on kz planes instead of nz, and
+// the full 3D spectrum is never written.
+struct BuildZParams {
+  BuildParams b;      // morphology, constants, window, mean, mode
+  FftAxis az;         // z-axis plan (n = nz)
+  uint32_t tx;        // columns per block
+  uint32_t zlo, kz;   // kept shifted planes
+  float2 *out;        // [nvol][kz][ny][nx]
+};
+
+__device__ __forceinline__ uint32_t igor(uint32_t j, uint32_t n);
+
+template <int MORPH>
+__global__ void __launch_bounds__(kFftThreads, 2) k_build_fft_z(BuildZParams p, const MaterialConsts *__restrict__ mcp) {
+  extern __shared__ float2 smem[];
+  __shared__ MaterialConsts mc;
+  load_consts(mc, mcp);
+  const BuildParams &b = p.b;
+  const uint32_t nz = p.az.n, TX = p.tx, S = TX + 1, nvol = b.nvol;
+  const size_t vsz = size_t(nz) * S;
+  float2 *bufa = smem, *bufb = smem + nvol * vsz;
+  const uint32_t nxt = (b.nx + TX - 1) / TX;
+  const uint32_t xt = blockIdx.x % nxt, y = blockIdx.x / nxt, x0 = xt * TX;
+  const bool use_conv = MORPH == 0 && b.conv && *b.neg == 0u;
+  __syncthreads();
+  for (uint32_t t = threadIdx.x; t < TX * nz; t += blockDim.x) {
+    const uint32_t l = t % TX, z = t / TX, x = x0 + l;
+    float2 v[6];
+    if (x < b.nx) {
+      const size_t i = (size_t(z) * b.ny + y) * b.nx + x;
+      if (use_conv)
+        voxel_values<MORPH, true>(b, mc, i, x, y, z, v);
+      else
+        voxel_values<MORPH, false>(b, mc, i, x, y, z, v);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) v[c] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+      if (uint32_t(c) < nvol) bufa[c * vsz + size_t(z) * S + l] = v[c];
+  }
+  __syncthreads();
+  const float2 *res = stockham(bufa, bufb, p.az, TX, S, nvol);
+  const size_t plane = size_t(b.nx) * b.ny;
+  for (uint32_t t = threadIdx.x; t < nvol * p.kz * TX; t += blockDim.x) {
+    const uint32_t l = t % TX, rest = t / TX;
+    const uint32_t q = rest % p.kz, v = rest / p.kz;
+    const uint32_t x = x0 + l;
+    if (x >= b.nx) continue;
+    const uint32_t u = igor(p.zlo + q, nz);
+    p.out[(size_t(v) * p.kz + q) * plane + size_t(y) * b.nx + x] = res[(size_t(v) * nz + u) * S + l];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // 3. DC replacement value per volume (src/cudaMain.cu:123-176): the mean of
 // the periodic neighbours of index 0 in the unshifted spectrum.  The Ewald
 // gather substitutes it wherever it reads index 0; the spectrum itself is
 // left untouched.
 // ---------------------------------------------------------------------------
-__global__ void k_dc(const float2 *__restrict__ spec, uint32_t nvol, size_t nvox, uint32_t nx, uint32_t ny, uint32_t nz,
-                     float2 *__restrict__ dc) {
+// The spectra are stored as planes: plane pz of volume v starts at
+// spec + v * vstride + pz * nx * ny.  p0, p1, pn are the planes holding the
+// unshifted z bins 0, 1 and nz-1.
+__global__ void k_dc(const float2 *__restrict__ spec, uint32_t nvol, size_t vstride, uint32_t nx, uint32_t ny,
+                     uint32_t nz, uint32_t p0, uint32_t p1, uint32_t pn, float2 *__restrict__ dc) {
   const uint32_t v = threadIdx.x;
   if (v >= nvol) return;
-  const float2 *P = spec + size_t(v) * nvox;
+  const size_t P = size_t(nx) * ny;
+  const float2 *V = spec + size_t(v) * vstride;
+  const float2 *Z0 = V + size_t(p0) * P;
   float2 s = make_float2(0.f, 0.f);
-  s = cadd(s, P[1 % nvox]);
-  s = cadd(s, P[nx % nvox]);
-  s = cadd(s, P[(nx - 1) % nvox]);
-  s = cadd(s, P[(size_t(ny - 1) * nx) % nvox]);
+  s = cadd(s, Z0[1]);
+  s = cadd(s, Z0[nx]);
+  s = cadd(s, Z0[nx - 1]);
+  s = cadd(s, Z0[size_t(ny - 1) * nx]);
   float cnt = 4.f;
   if (nz > 1) {
-    s = cadd(s, P[size_t(nx) * ny]);
-    s = cadd(s, P[size_t(nz - 1) * nx * ny]);
+    s = cadd(s, V[size_t(p1) * P]);
+    s = cadd(s, V[size_t(pn) * P]);
     cnt = 6.f;
   }
   dc[v] = make_float2(s.x / cnt, s.y / cnt);
@@ -514,10 +615,13 @@ __global__ void k_dc(const float2 *__restrict__ spec, uint32_t nvol, size_t nvox
 // between the two planes (:800-803).  Writes images[a][P].
 // ---------------------------------------------------------------------------
 struct EwaldParams {
-  const float2 *spec;     // [nvol][V]
+  const float2 *spec;     // [nvol][planes][ny][nx]
   const float2 *dc;       // [nvol]
   uint32_t nx, ny, nz;
-  size_t nvox;
+  size_t nvox;            // volume stride of spec (elements)
+  uint32_t zshifted;      // 1: plane q holds shifted z = zlo + q (nplanes planes); 0: plane = unshifted z
+  uint32_t zlo, nplanes;
+  unsigned int *errors;   // incremented when a needed plane is not stored
   uint32_t nbasis;        // 1..3
   uint32_t vol[3][3];     // vol[c][b]: volume holding component c of basis b
   uint32_t nangles;
@@ -594,12 +698,22 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
   const uint32_t zs[2] = {Z0, Z1};
   for (int pl = 0; pl < nplanes; ++pl) {
     const uint32_t uz = p.twod ? 0u : igor(zs[pl], p.nz);
-    const size_t idx = size_t(ux) + size_t(uy) * p.nx + size_t(uz) * p.nx * p.ny;
+    uint32_t pz = uz;
+    if (p.zshifted) {
+      pz = zs[pl] - p.zlo;
+      if (zs[pl] < p.zlo || pz >= p.nplanes) {  // the host's plane range missed this pixel
+        atomicAdd(p.errors, 1u);
+        for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
+        return;
+      }
+    }
+    const bool is_dc = ux == 0 && uy == 0 && uz == 0;
+    const size_t idx = size_t(ux) + size_t(uy) * p.nx + size_t(pz) * p.nx * p.ny;
     for (uint32_t b = 0; b < p.nbasis; ++b)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const uint32_t v = p.vol[c][b];
-        P[pl][c][b] = idx == 0 ? p.dc[v] : __ldg(&p.spec[size_t(v) * p.nvox + idx]);
+        P[pl][c][b] = is_dc ? p.dc[v] : __ldg(&p.spec[size_t(v) * p.nvox + idx]);
       }
     Q[pl][0] = p.kx + p.qx[X];
     Q[pl][1] = p.ky + p.qy[Y];

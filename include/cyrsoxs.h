@@ -111,6 +111,22 @@ CYR_API int cyr_simulate_device(const cyr_options *opt, const float *optical, co
 /* Device bytes the engine needs for one request with these options. */
 CYR_API int cyr_required_device_bytes(const cyr_options *opt, size_t *bytes);
 
+/*
+ * Shape of the engine's plan for these options: info[0] = spectrum volumes
+ * per energy (5 or 6 tensor entries, 3 for the MATERIAL frame), info[1] =
+ * z planes kept after the z FFT (nz when not pruned), info[2] = first kept
+ * shifted plane, info[3] = 1 when the z axis is pruned, info[4] = E angles,
+ * info[5] = k vectors.
+ */
+CYR_API int cyr_plan_info(const cyr_options *opt, uint32_t *info, uint32_t n);
+
+/*
+ * Device-side consistency errors counted since the last request started on
+ * this device (e.g. a detector pixel needed a z plane outside the kept
+ * range).  Waits for the device; 0 means none.
+ */
+CYR_API int cyr_device_errors(uint32_t *count);
+
 /* Releases the library's cached scratch space on the current device. */
 CYR_API int cyr_release_scratch(void);
 

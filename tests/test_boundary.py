@@ -93,7 +93,11 @@ def test_required_bytes_counts_the_tensor_volumes():
     opts = nat.Options(nx=64, ny=64, nz=16, num_material=2, energies=[280.0, 285.0], start_angle=0, end_angle=165,
                        increment_angle=15, phys_size=5.0)
     b = nat.required_device_bytes(opts)
-    assert b >= 5 * 64 * 64 * 16 * 8 + 12 * 64 * 64 * 4  # 5 complex volumes + 12 images
+    # 5 complex tensor volumes, pruned to at least the 3 planes around the DC bin, 12 images and the
+    # trigonometry-free copy of the Euler morphology (2 materials x float4)
+    conv = 2 * 64 * 64 * 16 * 16
+    lo = 5 * 3 * 64 * 64 * 8 + 12 * 64 * 64 * 4 + conv
+    assert lo <= b <= lo + 5 * 64 * 64 * 16 * 8 + (1 << 20)
 
 
 # ---------------------------------------------------------------------------
