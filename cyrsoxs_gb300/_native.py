@@ -77,6 +77,8 @@ def lib():
     L.cyr_required_device_bytes.argtypes = [opt_p, ctypes.POINTER(ctypes.c_size_t)]
     L.cyr_fft3d_device.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.c_void_p]
+    L.cyr_fft3d_device_static.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                          ctypes.c_uint32, ctypes.c_void_p]
     L.cyr_warp_affine_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
     L.cyr_plan_info.argtypes = [opt_p, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32]
@@ -178,6 +180,11 @@ def simulate_device(opts: Options, optical: np.ndarray, d_voxels: int, d_out: in
 
 def fft3d_device(d_data: int, nx: int, ny: int, nz: int, count: int = 1, stream: int = 0) -> None:
     check(lib().cyr_fft3d_device(ctypes.c_void_p(d_data), nx, ny, nz, count, ctypes.c_void_p(stream)))
+
+
+def fft3d_device_static(d_data: int, nx: int, ny: int, nz: int, count: int = 1, stream: int = 0) -> None:
+    """The allocation-free variant of fft3d_device (twiddles in a fixed device array)."""
+    check(lib().cyr_fft3d_device_static(ctypes.c_void_p(d_data), nx, ny, nz, count, ctypes.c_void_p(stream)))
 
 
 def warp_affine_device(d_src: int, d_dst: int, width: int, height: int, coeffs, stream: int = 0) -> None:

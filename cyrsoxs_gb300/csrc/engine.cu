@@ -1017,3 +1017,100 @@ int cyr_warp_affine_device(const float *d_src, float *d_dst, int width, int heig
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free FFT entry point.
+//
+// Some callers cannot allocate device memory at the point where they need the
+// transform: code running inside a memory pool or arena that owns every byte
+// of the device and forbids cudaMalloc/cudaFree, or a host that must not call
+// allocating routines on a latency-critical path.  cyr_fft3d_device
+// allocates its twiddle tables (cudaMalloc, once per length); this variant
+// keeps them in a fixed file-scope device array instead.  The array is part of
+// the library image: every GPU that loads the library holds its
+// kStaticTwiddleBytes until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr uint32_t kStaticMaxLength = 4096;  // per axis
+constexpr size_t kStaticTwiddleBytes = size_t(3) * kStaticMaxLength * sizeof(float2);  // 96 KiB
+__device__ __align__(256) float2 g_static_twiddles[3 * kStaticMaxLength];
+
+struct StaticTwiddleState {
+  float2 *dev_ptr = nullptr;  // device address of g_static_twiddles on this device
+  bool attrs = false;
+};
+std::mutex g_static_mu;
+std::map<int, StaticTwiddleState> g_static_state;
+}  // namespace
+
+extern "C" int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count,
+                                       void *stream) {
+  if (!d_data || nx < 1 || ny < 1 || nz < 1 || count < 1) return fail(CYR_ERR_ARGUMENT, "bad FFT arguments");
+  if (nx > kStaticMaxLength || ny > kStaticMaxLength || nz > kStaticMaxLength)
+    return fail(CYR_ERR_ARGUMENT, "cyr_fft3d_device_static: every axis must be at most %u long (got %u x %u x %u)",
+                kStaticMaxLength, nx, ny, nz);
+  if (count > 65535) return fail(CYR_ERR_ARGUMENT, "too many volumes in one call");
+  std::vector<uint32_t> r;
+  for (uint32_t n : {nx, ny, nz})
+    if (n > 1 && !factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u has a prime factor above 7", n);
+  int dev = 0;
+  CYR_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  StaticTwiddleState &stt = g_static_state[dev];
+  if (!stt.dev_ptr) {
+    // one-time set-up on this device (must precede any stream capture): the
+    // host-side name g_static_twiddles is not a device address
+    void *p = nullptr;
+    CYR_CUDA(cudaGetSymbolAddress(&p, g_static_twiddles));
+    stt.dev_ptr = static_cast<float2 *>(p);
+  }
+  if (!stt.attrs) {
+    const int smem = int(kFftSmemBudget);
+    CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    stt.attrs = true;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // The tables of this call replace the previous call's contents (every entry
+  // the passes read is written here, nothing relies on zeros).  Calls whose
+  // work overlaps on the GPU share the array and race.
+  const uint32_t dims[3] = {nx, ny, nz};
+  std::vector<float2> host(size_t(3) * kStaticMaxLength);
+  for (int a = 0; a < 3; ++a)
+    for (uint32_t m = 0; m < dims[a]; ++m) {
+      const double ang = -2.0 * kPi * double(m) / double(dims[a]);
+      host[size_t(a) * kStaticMaxLength + m] = make_float2(float(std::cos(ang)), float(std::sin(ang)));
+    }
+  // pageable source: the copy is staged before this call returns
+  CYR_CUDA(cudaMemcpyAsync(stt.dev_ptr, host.data(), kStaticTwiddleBytes, cudaMemcpyHostToDevice, st));
+  const size_t nvox = size_t(nx) * ny * nz;
+  for (int axis = 0; axis < 3; ++axis) {
+    const uint32_t n = dims[axis];
+    if (n == 1) continue;
+    FftPassParams p{};
+    p.data = static_cast<float2 *>(d_data);
+    p.nx = nx, p.ny = ny, p.nz = nz;
+    p.nvox = nvox;
+    factorize(n, r);
+    p.ax.n = n;
+    p.ax.log2n = 0;
+    if ((n & (n - 1)) == 0)
+      while ((1u << p.ax.log2n) < n) ++p.ax.log2n;
+    p.ax.nstages = uint32_t(r.size());
+    p.ax.radix_code = 0;
+    for (size_t i = 0; i < r.size(); ++i) p.ax.radix_code |= uint64_t(r[i]) << (4 * i);
+    p.ax.tw = stt.dev_ptr + size_t(axis) * kStaticMaxLength;
+    p.tx = fft_lines_per_block(n);
+    const size_t smem = size_t(2) * n * (p.tx + 1) * sizeof(float2);
+    if (smem > kFftSmemBudget) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u too large for one block", n);
+    const uint32_t tiles =
+        axis == 0 ? (ny * nz + p.tx - 1) / p.tx : ((nx + p.tx - 1) / p.tx) * (axis == 1 ? nz : ny);
+    const dim3 grid(tiles, count);
+    if (axis == 0) k_fft_pass<0><<<grid, kFftThreads, smem, st>>>(p);
+    if (axis == 1) k_fft_pass<1><<<grid, kFftThreads, smem, st>>>(p);
+    if (axis == 2) k_fft_pass<2><<<grid, kFftThreads, smem, st>>>(p);
+    CYR_CUDA(cudaGetLastError());
+  }
+  return CYR_OK;
+}

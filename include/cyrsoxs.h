@@ -141,6 +141,23 @@ CYR_API int cyr_release_scratch(void);
 CYR_API int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, void *stream);
 
 /*
+ * cyr_fft3d_device_static: the same transform as cyr_fft3d_device for callers
+ * that cannot allocate device memory (code inside a memory pool or arena that
+ * owns the device and forbids cudaMalloc/cudaFree, or latency-critical paths
+ * that must not call allocating routines).  It calls no cudaMalloc, cudaFree
+ * or allocating library routine: its twiddle tables live in a fixed 96 KiB
+ * device array that is part of the library image and that every GPU loading
+ * the library holds until the process exits.  Each axis may be at most 4096
+ * long; longer axes are rejected with CYR_ERR_ARGUMENT.  The first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  All calls share the array and
+ * each call rewrites it: calls whose work overlaps on the GPU race.
+ * This entry point has no counterpart in the reference.
+ */
+CYR_API int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count,
+                                    void *stream);
+
+/*
  * cyr_warp_affine_device: bilinear affine warp of a float [height][width]
  * image with the semantics of nppiWarpAffine_32f_C1R + NPPI_INTER_LINEAR
  * (src/cudaMain.cu:91-121, :858, :943).  coeffs is the 2x3 matrix mapping
