@@ -296,18 +296,20 @@ def main():
         step()
     torch.cuda.synchronize()
     kernels, dropped = _native.profile_end()
-    launches_per_step = sum(n for n, _ in kernels.values()) / prof_steps
+    launches_per_step = sum(n for n, _, _ in kernels.values()) / prof_steps
     info = _native.plan_info(opts)
     nvol, planes = info["nvol"], info["planes"]
     dom = max(kernels.items(), key=lambda kv: kv[1][1])
-    dom_name, (dom_n, dom_ms) = dom
+    dom_name, (_, dom_ms, dom_n) = dom
     peak, peak_kind = load_peaks()
     dom_bytes = algorithmic_bytes(dom_name, w, nvol, nang, planes)
     achieved = dom_bytes / (dom_ms / dom_n / 1000.0) / 1e9
     traffic = load_traffic(w.name).get(dom_name)
-    kernel_table = {k: {"launches_per_step": n / prof_steps, "ms_per_launch": ms / n,
-                        "gbs": (algorithmic_bytes(k, w, nvol, nang, planes) or 0) / (ms / n / 1000.0) / 1e9}
-                    for k, (n, ms) in kernels.items()}
+    # a "call" is one timed launch of the kernel's work (for Euler input the build kernels are
+    # launched as a converted/trigonometric pair of which one returns at entry)
+    kernel_table = {k: {"launches_per_step": n / prof_steps, "calls_per_step": c / prof_steps, "ms_per_call": ms / c,
+                        "gbs": (algorithmic_bytes(k, w, nvol, nang, planes) or 0) / (ms / c / 1000.0) / 1e9}
+                    for k, (n, ms, c) in kernels.items()}
 
     result = {
         "metric": METRIC, "value": value, "unit": "patterns/s", "n_gpus": world, "steps": args.steps,
@@ -328,6 +330,7 @@ def main():
         "kernels": kernel_table,
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "plan": info,
+        "autotune": _native.tuning_report().strip().splitlines(),
         "clocks": None,
     }
     if rank == 0:

@@ -83,9 +83,10 @@ def lib():
                                          ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
     L.cyr_plan_info.argtypes = [opt_p, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32]
     L.cyr_device_errors.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+    L.cyr_tuning_report.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.cyr_profile_begin.argtypes = [ctypes.c_uint32]
-    L.cyr_profile_end.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
-                                  ctypes.POINTER(ctypes.c_uint32)]
+    L.cyr_profile_end.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                  ctypes.POINTER(ctypes.c_double), ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
     L.cyr_stage_name.argtypes = [ctypes.c_uint32]
     L.cyr_stage_name.restype = ctypes.c_char_p
     L.cyr_num_stages.restype = ctypes.c_uint32
@@ -200,6 +201,12 @@ def plan_info(opts: Options) -> dict:
             "k": info[5]}
 
 
+def tuning_report() -> str:
+    buf = ctypes.create_string_buffer(8192)
+    check(lib().cyr_tuning_report(buf, 8192))
+    return buf.value.decode()
+
+
 def device_errors() -> int:
     n = ctypes.c_uint32(0)
     check(lib().cyr_device_errors(ctypes.byref(n)))
@@ -211,16 +218,17 @@ def profile_begin(max_launches: int = 65536) -> None:
 
 
 def profile_end():
-    """{kernel name: (launches, total ms)} for the launches since profile_begin, and the dropped count."""
+    """{kernel name: (launches, total ms, timed calls)} since profile_begin, and the dropped count."""
     n = int(lib().cyr_num_stages())
     launches = (ctypes.c_uint32 * n)()
+    calls = (ctypes.c_uint32 * n)()
     ms = (ctypes.c_double * n)()
     dropped = ctypes.c_uint32(0)
-    check(lib().cyr_profile_end(launches, ms, n, ctypes.byref(dropped)))
+    check(lib().cyr_profile_end(launches, calls, ms, n, ctypes.byref(dropped)))
     out = {}
     for i in range(n):
         if launches[i]:
-            out[lib().cyr_stage_name(i).decode()] = (int(launches[i]), float(ms[i]))
+            out[lib().cyr_stage_name(i).decode()] = (int(launches[i]), float(ms[i]), int(calls[i]))
     return out, int(dropped.value)
 
 

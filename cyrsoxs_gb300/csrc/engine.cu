@@ -130,15 +130,17 @@ struct Profiler {
   bool active = false;
   std::vector<cudaEvent_t> events;  // pairs
   std::vector<int> stage;           // stage of pair i
+  std::vector<int> count;           // kernel launches inside pair i
   size_t used = 0;                  // pairs recorded
   size_t dropped = 0;
-  int begin(int st, cudaStream_t s) {
+  int begin(int st, cudaStream_t s, int launches = 1) {
     if (!active) return -1;
     if (used >= stage.size()) {
-      ++dropped;
+      dropped += launches;
       return -1;
     }
     stage[used] = st;
+    count[used] = launches;
     cudaEventRecord(events[2 * used], s);
     return int(used++);
   }
@@ -147,9 +149,17 @@ struct Profiler {
   }
 };
 
+// Autotuned launch configuration of the fused build + z FFT per shape.
+struct ZTune {
+  bool stage = false;
+  uint32_t tx = 4;
+  float ms = 0.f;
+};
+
 struct DeviceContext {
   int device = -1;
   Profiler prof;
+  std::map<std::string, ZTune> ztune;  // key: nx,ny,nz,nmat,nvol,morphology
   std::mutex mu;
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
@@ -184,8 +194,19 @@ int setup_attrs(DeviceContext &ctx) {
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+#define CYR_WARP_Z_ATTR(V, T)                                                                                     \
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z_warp<0, true, V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));  \
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z_warp<0, false, V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z_warp<1, false, V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+#define CYR_WARP_Z_ATTR_V(V) CYR_WARP_Z_ATTR(V, 2) CYR_WARP_Z_ATTR(V, 4) CYR_WARP_Z_ATTR(V, 8)
+  CYR_WARP_Z_ATTR_V(4)
+  CYR_WARP_Z_ATTR_V(8)
+  CYR_WARP_Z_ATTR_V(16)
+#undef CYR_WARP_Z_ATTR_V
+#undef CYR_WARP_Z_ATTR
   CYR_CUDA(cudaEventCreateWithFlags(&ctx.last_use, cudaEventDisableTiming));
   ctx.attrs_done = true;
   return CYR_OK;
@@ -223,6 +244,48 @@ int make_axis(DeviceContext &ctx, uint32_t n, FftAxis &ax) {
   return get_twiddles(ctx, n, &ax.tw);
 }
 
+// One axis of the 3D FFT with the warp-level kernels (n = 128, 256, 512).
+template <int V>
+int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
+                    cudaStream_t st) {
+  constexpr uint32_t N = 32 * V;
+  const size_t nvox = size_t(nx) * ny * nz;
+  const float2 *tw = nullptr;
+  CYR_TRY(get_twiddles(ctx, N, &tw));
+  const int slot = ctx.prof.begin(kFftX + axis, st);
+  if (axis == 0) {
+    RowPassParams rp{data, uint32_t(size_t(ny) * nz * count), tw};
+    const size_t smem = (N + 8 * fpad_len(N)) * sizeof(float2);
+    k_fft_rows<V><<<(rp.rows + 7) / 8, 256, smem, st>>>(rp);
+  } else {
+    constexpr uint32_t TX = 8;
+    ColPassParams cp{};
+    cp.data = data;
+    cp.nx = nx;
+    cp.vstride = nvox;
+    if (axis == 1) {
+      cp.others = nz, cp.ostride = size_t(nx) * ny, cp.estride = nx;
+    } else {
+      cp.others = ny, cp.ostride = nx, cp.estride = nx * ny;
+    }
+    cp.tw = tw;
+    const size_t smem = (N + TX * line_stride(N, TX)) * sizeof(float2);
+    const dim3 grid(((nx + TX - 1) / TX) * cp.others, count);
+    k_fft_cols<V><<<grid, TX * 32, smem, st>>>(cp);
+  }
+  ctx.prof.end(slot, st);
+  CYR_CUDA(cudaGetLastError());
+  return CYR_OK;
+}
+
+int warp_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
+                  cudaStream_t st) {
+  const uint32_t n = axis == 0 ? nx : axis == 1 ? ny : nz;
+  if (n == 128) return warp_fft_pass_v<4>(ctx, data, nx, ny, nz, count, axis, st);
+  if (n == 256) return warp_fft_pass_v<8>(ctx, data, nx, ny, nz, count, axis, st);
+  return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st);
+}
+
 // In-place forward 3D FFT of `count` volumes.
 int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
           bool skip_z = false) {
@@ -231,13 +294,17 @@ int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t n
   for (int axis = 0; axis < (skip_z ? 2 : 3); ++axis) {
     const uint32_t n = dims[axis];
     if (n == 1) continue;
+    if (n == 128 || n == 256 || n == 512) {
+      CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st));
+      continue;
+    }
     FftPassParams p{};
     p.data = data;
     p.nx = nx, p.ny = ny, p.nz = nz;
     p.nvox = nvox;
     CYR_TRY(make_axis(ctx, n, p.ax));
     p.tx = fft_lines_per_block(n);
-    const size_t smem = size_t(2) * n * (p.tx + 1) * sizeof(float2);
+    const size_t smem = (size_t(2) * n * (p.tx + 1) + n) * sizeof(float2);
     if (smem > kFftSmemBudget) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u too large for one block", n);
     uint32_t tiles;
     if (axis == 0) {
@@ -279,9 +346,19 @@ struct Plan {
   // z pruning: the spectra keep shifted planes [zlo, zlo + kz) only
   bool pruned = false;
   uint32_t zlo = 0, kz = 0, ztx = 1;
+  bool zwarp = false;                   // warp-FFT form of the fused kernel
+  bool zstage = false;                  // ... with the morphology tile staged in shared memory
+  std::vector<ZTune> zcands;            // autotuning candidates of the warp form
   size_t vstride = 0;                   // elements per spectrum volume
   uint32_t p0 = 0, p1 = 0, pn = 0;      // planes of unshifted z bins 0, 1, nz-1
 };
+
+// Dynamic shared memory of k_build_fft_z_warp: twiddles, lines, optional tile.
+inline size_t zwarp_smem(uint32_t nz, uint32_t nvol, uint32_t tx, uint32_t nmat, bool stage) {
+  size_t f2 = nz + size_t(nvol) * tx * line_stride(nz, tx);
+  f2 += f2 & 1;  // the float4 tile starts 16-byte aligned
+  return f2 * sizeof(float2) + (stage ? size_t(nmat) * nz * tx * sizeof(float4) : 0);
+}
 
 inline uint32_t igor_host(uint32_t j, uint32_t n) { return j <= n / 2 ? n / 2 - j : n + n / 2 - j; }
 
@@ -426,11 +503,27 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
   pl.euler = o->morphology_type == 0;
   pl.vstride = pl.nvox;
   pl.p0 = 0, pl.p1 = 1 % pl.nz, pl.pn = pl.nz - 1;
-  if (!pl.twod) {
+  if (!pl.twod && (pl.nz == 128 || pl.nz == 256 || pl.nz == 512)) {
+    // warp-FFT form: TX columns per block, with or without the morphology
+    // tile staged through shared memory.  The candidates that fit are timed
+    // on the first request of this shape (run_request) and the fastest kept.
+    for (bool stage : {false, true})
+      for (uint32_t t : {2u, 4u, 8u})
+        if (zwarp_smem(pl.nz, pl.nvol, t, pl.nmat, stage) <= (stage ? 120 : 100) * 1024)
+          pl.zcands.push_back({stage, t, 0.f});
+    pl.zstage = false;
+    pl.ztx = 4;
+    for (const ZTune &c : pl.zcands)
+      if (!c.stage && c.tx <= 4) pl.ztx = c.tx;
+    pl.pruned = true;
+    pl.zwarp = true;
+    kept_planes(o, pl);
+    pl.vstride = size_t(pl.kz) * pl.npix;
+  } else if (!pl.twod) {
     // fused build + z FFT: lines per block so that two 512-thread blocks fit an SM
     uint32_t tx = 16;
-    while (tx > 1 && size_t(2) * pl.nvol * pl.nz * (tx + 1) * sizeof(float2) > 104 * 1024) tx /= 2;
-    if (size_t(2) * pl.nvol * pl.nz * (tx + 1) * sizeof(float2) <= kFftSmemBudget) {
+    while (tx > 1 && (size_t(2) * pl.nvol * pl.nz * (tx + 1) + pl.nz) * sizeof(float2) > 104 * 1024) tx /= 2;
+    if ((size_t(2) * pl.nvol * pl.nz * (tx + 1) + pl.nz) * sizeof(float2) <= kFftSmemBudget) {
       pl.pruned = true;
       pl.ztx = tx;
       kept_planes(o, pl);
@@ -640,22 +733,97 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       zp.zlo = pl.zlo;
       zp.kz = pl.kz;
       zp.out = spec;
-      const size_t smem = size_t(2) * bp.nvol * pl.nz * (pl.ztx + 1) * sizeof(float2);
-      const dim3 grid((pl.nx + pl.ztx - 1) / pl.ztx * pl.ny);
-      slot = ctx.prof.begin(kBuildZ, st);
-      if (o->morphology_type == 0)
-        k_build_fft_z<0><<<grid, kFftThreads, smem, st>>>(zp, mce);
-      else
-        k_build_fft_z<1><<<grid, kFftThreads, smem, st>>>(zp, mce);
-      ctx.prof.end(slot, st);
+      if (pl.zwarp) {
+        auto launch_warp = [&](const ZTune &cfg) {
+          zp.stage = cfg.stage ? 1u : 0u;
+          zp.tx = cfg.tx;
+          const dim3 g((pl.nx + cfg.tx - 1) / cfg.tx * pl.ny);
+          const size_t smem = zwarp_smem(pl.nz, bp.nvol, cfg.tx, pl.nmat, cfg.stage);
+#define CYR_LAUNCH_WARP_ZT(V, T)                                                   \
+  if (o->morphology_type == 0) {                                                   \
+    k_build_fft_z_warp<0, true, V, T><<<g, 256, smem, st>>>(zp, mce);              \
+    k_build_fft_z_warp<0, false, V, T><<<g, 256, smem, st>>>(zp, mce);             \
+  } else {                                                                         \
+    k_build_fft_z_warp<1, false, V, T><<<g, 256, smem, st>>>(zp, mce);             \
+  }
+#define CYR_LAUNCH_WARP_Z(V)         \
+  if (cfg.tx == 2) {                 \
+    CYR_LAUNCH_WARP_ZT(V, 2)         \
+  } else if (cfg.tx == 4) {          \
+    CYR_LAUNCH_WARP_ZT(V, 4)         \
+  } else {                           \
+    CYR_LAUNCH_WARP_ZT(V, 8)         \
+  }
+          if (pl.nz == 128) {
+            CYR_LAUNCH_WARP_Z(4)
+          } else if (pl.nz == 256) {
+            CYR_LAUNCH_WARP_Z(8)
+          } else {
+            CYR_LAUNCH_WARP_Z(16)
+          }
+#undef CYR_LAUNCH_WARP_Z
+#undef CYR_LAUNCH_WARP_ZT
+        };
+        char key[96];
+        std::snprintf(key, sizeof key, "%u,%u,%u,%u,%u,%u", pl.nx, pl.ny, pl.nz, pl.nmat, bp.nvol,
+                      o->morphology_type);
+        auto it = ctx.ztune.find(key);
+        if (it == ctx.ztune.end() && pl.zcands.size() > 1 && !ctx.prof.active) {
+          // autotune: time every candidate once on this energy; the last one's
+          // output stays in `spec` and is used
+          std::vector<cudaEvent_t> ev(2 * pl.zcands.size());
+          for (auto &e : ev) CYR_CUDA(cudaEventCreate(&e));
+          for (size_t c = 0; c < pl.zcands.size(); ++c) {
+            CYR_CUDA(cudaEventRecord(ev[2 * c], st));
+            launch_warp(pl.zcands[c]);
+            CYR_CUDA(cudaEventRecord(ev[2 * c + 1], st));
+          }
+          CYR_CUDA(cudaGetLastError());
+          CYR_CUDA(cudaEventSynchronize(ev.back()));
+          ZTune best = pl.zcands[0];
+          best.ms = 1e30f;
+          for (size_t c = 0; c < pl.zcands.size(); ++c) {
+            float ms = 0.f;
+            CYR_CUDA(cudaEventElapsedTime(&ms, ev[2 * c], ev[2 * c + 1]));
+            if (ms < best.ms) best = pl.zcands[c], best.ms = ms;
+          }
+          for (auto &e : ev) cudaEventDestroy(e);
+          ctx.ztune[key] = best;
+          launch_warp(best);  // the kept output must come from a full, ordered launch of the chosen form
+        } else {
+          ZTune cfg;
+          if (it != ctx.ztune.end()) {
+            cfg = it->second;
+          } else {
+            cfg.stage = pl.zstage;
+            cfg.tx = pl.ztx;
+          }
+          slot = ctx.prof.begin(kBuildZ, st, o->morphology_type == 0 ? 2 : 1);
+          launch_warp(cfg);
+          ctx.prof.end(slot, st);
+        }
+      } else {
+        const dim3 grid((pl.nx + pl.ztx - 1) / pl.ztx * pl.ny);
+        slot = ctx.prof.begin(kBuildZ, st, o->morphology_type == 0 ? 2 : 1);
+        const size_t smem = (size_t(2) * bp.nvol * pl.nz * (pl.ztx + 1) + pl.nz) * sizeof(float2);
+        if (o->morphology_type == 0) {
+          k_build_fft_z<0, true><<<grid, kFftThreads, smem, st>>>(zp, mce);
+          k_build_fft_z<0, false><<<grid, kFftThreads, smem, st>>>(zp, mce);
+        } else {
+          k_build_fft_z<1, false><<<grid, kFftThreads, smem, st>>>(zp, mce);
+        }
+        ctx.prof.end(slot, st);
+      }
       CYR_CUDA(cudaGetLastError());
       CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.kz, bp.nvol, st, true));
     } else {
-      slot = ctx.prof.begin(kBuild, st);
-      if (o->morphology_type == 0)
-        k_build<0><<<build_blocks, 256, 0, st>>>(bp, mce);
-      else
-        k_build<1><<<build_blocks, 256, 0, st>>>(bp, mce);
+      slot = ctx.prof.begin(kBuild, st, o->morphology_type == 0 ? 2 : 1);
+      if (o->morphology_type == 0) {
+        k_build<0, true><<<build_blocks, 256, 0, st>>>(bp, mce);
+        k_build<0, false><<<build_blocks, 256, 0, st>>>(bp, mce);
+      } else {
+        k_build<1, false><<<build_blocks, 256, 0, st>>>(bp, mce);
+      }
       ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());
       CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, bp.nvol, st));
@@ -782,6 +950,24 @@ int cyr_plan_info(const cyr_options *opt, uint32_t *info, uint32_t n) {
   CYR_TRY(make_plan(opt, dummy.data(), pl));
   const uint32_t v[6] = {pl.nvol, pl.pruned ? pl.kz : pl.nz, pl.zlo, pl.pruned ? 1u : 0u, pl.nang, pl.nk};
   for (uint32_t i = 0; i < n && i < 6; ++i) info[i] = v[i];
+  return CYR_OK;
+}
+
+int cyr_tuning_report(char *buf, size_t len) {
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::string r;
+  for (const auto &kv : ctx->ztune) {
+    char line[160];
+    std::snprintf(line, sizeof line, "build_fft_z[%s]: stage=%d tx=%u %.3f ms\n", kv.first.c_str(),
+                  kv.second.stage ? 1 : 0, kv.second.tx, kv.second.ms);
+    r += line;
+  }
+  if (buf && len) {
+    std::strncpy(buf, r.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
   return CYR_OK;
 }
 
@@ -923,9 +1109,9 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
     const MaterialConsts *mce = reinterpret_cast<const MaterialConsts *>(dp + pl.off_mc) + energy_id;
     const uint32_t blocks = uint32_t(std::min<size_t>((pl.nvox + 255) / 256, 65535));
     if (opt->morphology_type == 0)
-      k_build<0><<<blocks, 256, 0, st>>>(bp, mce);
+      k_build<0, false><<<blocks, 256, 0, st>>>(bp, mce);
     else
-      k_build<1><<<blocks, 256, 0, st>>>(bp, mce);
+      k_build<1, false><<<blocks, 256, 0, st>>>(bp, mce);
     if (cudaGetLastError() != cudaSuccess) {
       rc = fail(CYR_ERR_CUDA, "polarization kernel launch failed");
       break;
@@ -954,13 +1140,14 @@ int cyr_profile_begin(uint32_t max_launches) {
     p.events.push_back(e);
   }
   p.stage.assign(want, -1);
+  p.count.assign(want, 1);
   p.used = 0;
   p.dropped = 0;
   p.active = true;
   return CYR_OK;
 }
 
-int cyr_profile_end(uint32_t *launches, double *ms, uint32_t nstages, uint32_t *dropped) {
+int cyr_profile_end(uint32_t *launches, uint32_t *calls, double *ms, uint32_t nstages, uint32_t *dropped) {
   DeviceContext *ctx = nullptr;
   CYR_TRY(get_context(&ctx));
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -968,6 +1155,7 @@ int cyr_profile_end(uint32_t *launches, double *ms, uint32_t nstages, uint32_t *
   p.active = false;
   for (uint32_t i = 0; i < nstages; ++i) {
     if (launches) launches[i] = 0;
+    if (calls) calls[i] = 0;
     if (ms) ms[i] = 0.0;
   }
   for (size_t i = 0; i < p.used; ++i) {
@@ -976,7 +1164,8 @@ int cyr_profile_end(uint32_t *launches, double *ms, uint32_t nstages, uint32_t *
     CYR_CUDA(cudaEventElapsedTime(&t, p.events[2 * i], p.events[2 * i + 1]));
     const int s = p.stage[i];
     if (s >= 0 && uint32_t(s) < nstages) {
-      if (launches) launches[s] += 1;
+      if (launches) launches[s] += uint32_t(p.count[i]);
+      if (calls) calls[s] += 1;
       if (ms) ms[s] += t;
     }
   }
@@ -1102,7 +1291,7 @@ extern "C" int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, u
     for (size_t i = 0; i < r.size(); ++i) p.ax.radix_code |= uint64_t(r[i]) << (4 * i);
     p.ax.tw = stt.dev_ptr + size_t(axis) * kStaticMaxLength;
     p.tx = fft_lines_per_block(n);
-    const size_t smem = size_t(2) * n * (p.tx + 1) * sizeof(float2);
+    const size_t smem = (size_t(2) * n * (p.tx + 1) + n) * sizeof(float2);
     if (smem > kFftSmemBudget) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u too large for one block", n);
     const uint32_t tiles =
         axis == 0 ? (ny * nz + p.tx - 1) / p.tx : ((nx + p.tx - 1) / p.tx) * (axis == 1 ? nz : ny);

@@ -88,16 +88,18 @@ __device__ __forceinline__ void director(float4 s, float &sx, float &sy, float &
 // Tensor entries of one voxel.  With CONV the morphology has been converted
 // to the vector form u = sqrt(phi_a) s, phi_ui (phi_a s_i s_j = u_i u_j),
 // which needs no trigonometry per energy.
+// `base` points at material 0 of the voxel, material m at base + m * mstride
+// (global memory, or a tile staged in shared memory).
 template <int MORPH, bool CONV>
-__device__ __forceinline__ void nt_entries(const BuildParams &p, const MaterialConsts &mc, size_t i, float2 nt[6]) {
+__device__ __forceinline__ void nt_entries_at(const BuildParams &p, const MaterialConsts &mc, const float4 *base,
+                                              size_t mstride, float2 nt[6]) {
 #pragma unroll
   for (int q = 0; q < 6; ++q) nt[q] = make_float2(0.f, 0.f);
-  const float4 *src = CONV ? p.conv : p.vox;
   for (uint32_t m0 = 0; m0 < p.nmat; m0 += 4) {
     float4 sv[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u)  // issue the loads of up to 4 materials before using them
-      if (m0 + u < p.nmat) sv[u] = __ldg(&src[(m0 + u) * p.nvox + i]);
+      if (m0 + u < p.nmat) sv[u] = base[(m0 + u) * mstride];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (m0 + u >= p.nmat) break;
@@ -121,6 +123,11 @@ __device__ __forceinline__ void nt_entries(const BuildParams &p, const MaterialC
       nt[4] = cfma(pyz, D, nt[4]);
     }
   }
+}
+
+template <int MORPH, bool CONV>
+__device__ __forceinline__ void nt_entries(const BuildParams &p, const MaterialConsts &mc, size_t i, float2 nt[6]) {
+  nt_entries_at<MORPH, CONV>(p, mc, (CONV ? p.conv : p.vox) + i, p.nvox, nt);
 }
 
 // Volume moments of the morphology, per material, in double:
@@ -216,11 +223,20 @@ __global__ void k_entry_means(const double *__restrict__ mom, uint32_t nmat, siz
 // entries xx xy xz yy yz [zz] (nvol of them), mode 1 the polarization
 // p = Nt E (uniaxial.h:106-151), rotated by R^T in the MATERIAL frame
 // (:163-165); the volume mean is subtracted when p.mean is set.
+__device__ __forceinline__ void values_from_nt(const BuildParams &p, float2 nt[6], uint32_t x, uint32_t y, uint32_t z,
+                                               float2 out[6]);
+
 template <int MORPH, bool CONV>
 __device__ __forceinline__ void voxel_values(const BuildParams &p, const MaterialConsts &mc, size_t i, uint32_t x,
                                              uint32_t y, uint32_t z, float2 out[6]) {
   float2 nt[6];
   nt_entries<MORPH, CONV>(p, mc, i, nt);
+  values_from_nt(p, nt, x, y, z, out);
+}
+
+// Window, mean removal and (mode 1) the E / R^T maps applied to a voxel's tensor.
+__device__ __forceinline__ void values_from_nt(const BuildParams &p, float2 nt[6], uint32_t x, uint32_t y, uint32_t z,
+                                               float2 out[6]) {
   const float w = p.hann_x ? p.hann_x[x] * p.hann_y[y] * p.hann_z[z] : 1.f;
   if (p.mode == 0) {
 #pragma unroll
@@ -266,20 +282,22 @@ __device__ __forceinline__ void load_consts(MaterialConsts &dst, const MaterialC
   for (int t = threadIdx.x; t < int(sizeof(MaterialConsts) / 4); t += blockDim.x) d[t] = s[t];
 }
 
-template <int MORPH>
+// CONV selects the converted (trigonometry-free) morphology; for Euler input
+// both instantiations are launched and the one that does not match the
+// device-side flag returns at once.
+__device__ __forceinline__ bool conv_selected(const BuildParams &p) { return p.conv && *p.neg == 0u; }
+
+template <int MORPH, bool CONV>
 __global__ void __launch_bounds__(256) k_build(BuildParams p, const MaterialConsts *__restrict__ mcp) {
+  if (MORPH == 0 && conv_selected(p) != CONV) return;
   __shared__ MaterialConsts mc;
   load_consts(mc, mcp);
   __syncthreads();
-  const bool use_conv = MORPH == 0 && p.conv && *p.neg == 0u;
   const size_t stride = size_t(gridDim.x) * blockDim.x;
   for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
     const uint32_t x = uint32_t(i % p.nx), y = uint32_t((i / p.nx) % p.ny), z = uint32_t(i / (size_t(p.nx) * p.ny));
     float2 v[6];
-    if (use_conv)
-      voxel_values<MORPH, true>(p, mc, i, x, y, z, v);
-    else
-      voxel_values<MORPH, false>(p, mc, i, x, y, z, v);
+    voxel_values<MORPH, CONV>(p, mc, i, x, y, z, v);
 #pragma unroll
     for (int c = 0; c < 6; ++c)
       if (uint32_t(c) < p.nvol) p.out[c * p.nvox + i] = v[c];
@@ -379,6 +397,7 @@ __device__ __forceinline__ void stockham_stage(const float2 *__restrict__ src, f
   const uint32_t m = n / R;               // butterflies per line
   const uint32_t twstep = n / (ns * R);   // W_{ns R}^{k r} = W_n^{k r twstep}
   const uint32_t jobs = m * lines * nv;
+  const uint32_t mS = m * S, nsS = ns * S;
   for (uint32_t job = threadIdx.x; job < jobs; job += blockDim.x) {
     const uint32_t l = job & (lines - 1), rest = job >> lg_lines;  // lines is a power of two
     uint32_t j, v, k, q;
@@ -387,28 +406,35 @@ __device__ __forceinline__ void stockham_stage(const float2 *__restrict__ src, f
     } else {
       j = rest % m, v = rest / m, k = j % ns, q = j / ns;
     }
-    const size_t vb = size_t(v) * n;
+    const uint32_t vb = v * n;  // shared-memory offsets fit in 32 bits
+    const uint32_t in0 = (vb + j) * S + l;
     float2 w[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) w[r] = src[(vb + j + r * m) * S + l];
+    for (int r = 0; r < R; ++r) w[r] = src[in0 + r * mS];
     if (ns > 1) {
+      const uint32_t t1 = k * twstep;
 #pragma unroll
-      for (int r = 1; r < R; ++r) w[r] = cmul(w[r], __ldg(&tw[k * r * twstep]));
+      for (int r = 1; r < R; ++r) w[r] = cmul(w[r], tw[t1 * r]);
     }
     if (R == 2) dft2(w);
     if (R == 4) dft4(w[0], w[1], w[2], w[3]);
     if (R == 8) dft8(w);
     if (R == 3 || R == 5 || R == 7) dft_odd<(R == 2 || R == 4 || R == 8) ? 3 : R>(w);
-    const uint32_t base = q * ns * R + k;
+    const uint32_t out0 = (vb + q * ns * R + k) * S + l;
 #pragma unroll
-    for (int r = 0; r < R; ++r) dst[(vb + base + r * ns) * S + l] = w[r];
+    for (int r = 0; r < R; ++r) dst[out0 + r * nsS] = w[r];
   }
+}
+
+// Copies the twiddle table W_n^m (m < n) into shared memory.
+__device__ __forceinline__ void stage_twiddles(float2 *dst, const float2 *__restrict__ src, uint32_t n) {
+  for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) dst[t] = __ldg(&src[t]);
 }
 
 // Runs all stages; returns the buffer holding the result.  `lines` must be a
 // power of two.
-__device__ __forceinline__ float2 *stockham(float2 *a, float2 *b, const FftAxis &ax, uint32_t lines, uint32_t S,
-                                            uint32_t nv = 1) {
+__device__ __forceinline__ float2 *stockham(float2 *a, float2 *b, const FftAxis &ax, const float2 *tw,
+                                            uint32_t lines, uint32_t S, uint32_t nv = 1) {
   const bool pow2 = ax.log2n != 0;
   const uint32_t lg_lines = 31 - __clz(lines);
   uint32_t ns = 1, lg_ns = 0;
@@ -417,12 +443,12 @@ __device__ __forceinline__ float2 *stockham(float2 *a, float2 *b, const FftAxis 
     const uint32_t lg_r = R == 8 ? 3 : R == 4 ? 2 : 1;
     const uint32_t lg_m = pow2 ? ax.log2n - lg_r : 0;
     switch (R) {
-      case 8: stockham_stage<8>(a, b, ax.n, ns, lines, nv, S, ax.tw, pow2, lg_lines, lg_m, lg_ns); break;
-      case 4: stockham_stage<4>(a, b, ax.n, ns, lines, nv, S, ax.tw, pow2, lg_lines, lg_m, lg_ns); break;
-      case 2: stockham_stage<2>(a, b, ax.n, ns, lines, nv, S, ax.tw, pow2, lg_lines, lg_m, lg_ns); break;
-      case 3: stockham_stage<3>(a, b, ax.n, ns, lines, nv, S, ax.tw, false, lg_lines, 0, 0); break;
-      case 5: stockham_stage<5>(a, b, ax.n, ns, lines, nv, S, ax.tw, false, lg_lines, 0, 0); break;
-      default: stockham_stage<7>(a, b, ax.n, ns, lines, nv, S, ax.tw, false, lg_lines, 0, 0); break;
+      case 8: stockham_stage<8>(a, b, ax.n, ns, lines, nv, S, tw, pow2, lg_lines, lg_m, lg_ns); break;
+      case 4: stockham_stage<4>(a, b, ax.n, ns, lines, nv, S, tw, pow2, lg_lines, lg_m, lg_ns); break;
+      case 2: stockham_stage<2>(a, b, ax.n, ns, lines, nv, S, tw, pow2, lg_lines, lg_m, lg_ns); break;
+      case 3: stockham_stage<3>(a, b, ax.n, ns, lines, nv, S, tw, false, lg_lines, 0, 0); break;
+      case 5: stockham_stage<5>(a, b, ax.n, ns, lines, nv, S, tw, false, lg_lines, 0, 0); break;
+      default: stockham_stage<7>(a, b, ax.n, ns, lines, nv, S, tw, false, lg_lines, 0, 0); break;
     }
     __syncthreads();
     float2 *t = a;
@@ -458,12 +484,11 @@ template <int AXIS>
 __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
   extern __shared__ float2 smem[];
   const uint32_t n = p.ax.n, TX = p.tx, S = TX + 1;
-  float2 *bufa = smem, *bufb = smem + size_t(n) * S;
-  float2 *vol = p.data + size_t(blockIdx.y) * p.nvox;
-  // Tile geometry: line l of this tile starts at base + l * lstep; element i at + i * estep.
+  float2 *bufa = smem, *bufb = smem + n * S, *tws = smem + 2 * n * S;
+  // Tile geometry: line l starts at tile + l * lstep; element i at + i * estep
+  // (offsets inside one volume fit in 32 bits).
   size_t base;
-  uint32_t valid;  // number of valid lines in this tile
-  size_t lstep, estep;
+  uint32_t valid, lstep, estep;
   if (AXIS == 0) {
     const uint32_t rows = p.ny * p.nz;
     const uint32_t r0 = blockIdx.x * TX;
@@ -482,9 +507,10 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
       estep = p.nx;
     } else {
       base = size_t(other) * p.nx + x0;  // other = y
-      estep = size_t(p.nx) * p.ny;
+      estep = p.nx * p.ny;
     }
   }
+  float2 *tile = p.data + size_t(blockIdx.y) * p.nvox + base;
   const uint32_t total = n * TX;
   for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
     uint32_t l, i;
@@ -495,13 +521,14 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
     }
     float2 *dst = &bufa[i * S + l];
     if (l < valid)
-      cp_async8(dst, &vol[base + l * lstep + i * estep]);
+      cp_async8(dst, &tile[l * lstep + i * estep]);
     else
       *dst = make_float2(0.f, 0.f);
   }
+  stage_twiddles(tws, p.ax.tw, n);
   cp_async_wait_all();
   __syncthreads();
-  const float2 *res = stockham(bufa, bufb, p.ax, TX, S);
+  const float2 *res = stockham(bufa, bufb, p.ax, tws, TX, S);
   for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
     uint32_t l, i;
     if (AXIS == 0) {
@@ -509,7 +536,169 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
     } else {
       l = t % TX, i = t / TX;
     }
-    if (l < valid) vol[base + l * lstep + i * estep] = res[i * S + l];
+    if (l < valid) tile[l * lstep + i * estep] = res[i * S + l];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-level FFT for power-of-two lengths N = 32 V (V = 4, 8, 16).
+//
+// One warp owns one line.  Lane t holds x[t + 32 i] in v[i] (natural order)
+// on entry and X[t + 32 i] on exit.  Each Stockham stage of radix R <= V runs
+// V / R butterflies per lane on registers; between stages the lanes exchange
+// through the warp's own line in shared memory (padded p -> p + p / 8, which
+// keeps the stride-R and stride-1 patterns free of bank conflicts), so only
+// __syncwarp is needed.  The last stage's outputs land in natural order in
+// registers.  Twiddles W_N^m come from a shared table generated in FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t fpad(uint32_t p) { return p + (p >> 3); }
+__host__ __device__ constexpr uint32_t fpad_len(uint32_t n) { return n + (n >> 3) + 1; }
+// Stride between the padded lines of TX interleaved columns: congruent to
+// 16 / TX modulo 16, so a half-warp touching TX columns x (16 / TX)
+// consecutive positions hits 16 distinct 8-byte bank pairs.
+__host__ __device__ constexpr uint32_t line_stride(uint32_t n, uint32_t tx) {
+  return ((fpad_len(n) + 15u) & ~15u) + (tx >= 16 ? 0u : 16u / tx);
+}
+
+template <int V>
+struct WarpPlan {
+  static constexpr int N = 32 * V;
+  static constexpr int LOG2N = V == 4 ? 7 : V == 8 ? 8 : 9;
+  // radices: as many 8s as V allows, then one 4 or 2 for the remainder
+  static constexpr int MAXR = V >= 8 ? 8 : V;
+  static constexpr int LOGMAXR = MAXR == 8 ? 3 : MAXR == 4 ? 2 : 1;
+  static constexpr int NFULL = LOG2N / LOGMAXR;
+  static constexpr int REM = LOG2N - NFULL * LOGMAXR;  // 0, 1 or 2
+  static constexpr int NSTAGES = NFULL + (REM ? 1 : 0);
+  __host__ __device__ static constexpr int radix(int s) { return s < NFULL ? MAXR : (REM == 2 ? 4 : 2); }
+};
+
+template <int V, int R, int NS, bool LAST>
+__device__ __forceinline__ void warp_stage(float2 (&v)[V], float2 *line, const float2 *__restrict__ tw,
+                                           uint32_t lane) {
+  constexpr int N = 32 * V;
+  constexpr int B = V / R;          // butterflies per lane
+  constexpr int TWS = N / (NS * R); // twiddle stride
+#pragma unroll
+  for (int q = 0; q < B; ++q) {
+    const uint32_t j = lane + 32 * q;
+    const uint32_t k = j & (NS - 1);
+    float2 w[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) w[r] = v[q + r * B];
+    if (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) w[r] = cmul(w[r], tw[k * r * TWS]);
+    }
+    if (R == 2) dft2(w);
+    if (R == 4) dft4(w[0], w[1], w[2], w[3]);
+    if (R == 8) dft8(w);
+    if (LAST) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[q + r * B] = w[r];  // position j + r N/R: natural order
+    } else {
+      const uint32_t base = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) line[fpad(base + r * NS)] = w[r];
+    }
+  }
+  if (!LAST) {
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < V; ++i) v[i] = line[fpad(lane + 32 * i)];
+    __syncwarp();
+  }
+}
+
+template <int V, int S, int NS>
+__device__ __forceinline__ void warp_fft_from(float2 (&v)[V], float2 *line, const float2 *tw, uint32_t lane) {
+  using P = WarpPlan<V>;
+  if constexpr (S < P::NSTAGES) {
+    constexpr int R = P::radix(S);
+    warp_stage<V, R, NS, S + 1 == P::NSTAGES>(v, line, tw, lane);
+    warp_fft_from<V, S + 1, NS * R>(v, line, tw, lane);
+  }
+}
+
+template <int V>
+__device__ __forceinline__ void warp_fft(float2 (&v)[V], float2 *line, const float2 *tw, uint32_t lane) {
+  warp_fft_from<V, 0, 1>(v, line, tw, lane);
+}
+
+// Row pass (x axis): one warp per contiguous row, straight from and to HBM.
+struct RowPassParams {
+  float2 *data;
+  uint32_t rows;   // rows in all volumes
+  const float2 *tw;
+};
+
+template <int V>
+__global__ void __launch_bounds__(256) k_fft_rows(RowPassParams p) {
+  constexpr int N = 32 * V;
+  extern __shared__ float2 smem[];
+  float2 *tws = smem;                              // N
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float2 *line = smem + N + warp * fpad_len(N);
+  for (uint32_t t = threadIdx.x; t < N; t += blockDim.x) tws[t] = __ldg(&p.tw[t]);
+  __syncthreads();
+  const uint32_t row = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (row >= p.rows) return;
+  float2 *r = p.data + size_t(row) * N;
+  float2 v[V];
+#pragma unroll
+  for (int i = 0; i < V; ++i) v[i] = r[lane + 32 * i];
+  warp_fft<V>(v, line, tws, lane);
+#pragma unroll
+  for (int i = 0; i < V; ++i) r[lane + 32 * i] = v[i];
+}
+
+// Column pass (y or z axis): a block owns TX = (warps) consecutive x columns
+// of one (plane or row, volume); the tile [N][TX] is loaded with cp.async in
+// rows of TX * 8 bytes into per-column padded lines, each warp transforms one
+// column, and the tile is stored back in rows.
+struct ColPassParams {
+  float2 *data;
+  uint32_t nx;         // columns per row
+  uint32_t others;     // lines per volume / nx (y: planes, z: ny)
+  size_t vstride;      // elements per volume
+  size_t ostride;      // stride between successive "other" indices
+  uint32_t estride;    // stride between successive elements of a column
+  const float2 *tw;
+};
+
+template <int V>
+__global__ void __launch_bounds__(256) k_fft_cols(ColPassParams p) {
+  constexpr uint32_t N = 32 * V, TX = 8, L = line_stride(N, TX);
+  extern __shared__ float2 smem[];
+  float2 *tws = smem, *tile = smem + N;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t nxt = (p.nx + TX - 1) / TX;
+  const uint32_t xt = blockIdx.x % nxt, other = blockIdx.x / nxt, x0 = xt * TX;
+  const uint32_t valid = min(TX, p.nx - x0);
+  float2 *g = p.data + size_t(blockIdx.y) * p.vstride + size_t(other) * p.ostride + x0;
+  const uint32_t l = threadIdx.x % TX, i0 = threadIdx.x / TX;  // compile-time TX: shifts
+  constexpr uint32_t ISTEP = 256 / TX;
+  if (l < valid) {
+#pragma unroll 4
+    for (uint32_t i = i0; i < N; i += ISTEP) cp_async8(&tile[l * L + fpad(i)], &g[l + i * p.estride]);
+  } else {
+    for (uint32_t i = i0; i < N; i += ISTEP) tile[l * L + fpad(i)] = make_float2(0.f, 0.f);
+  }
+  for (uint32_t t = threadIdx.x; t < N; t += blockDim.x) tws[t] = __ldg(&p.tw[t]);
+  cp_async_wait_all();
+  __syncthreads();
+  float2 *line = tile + warp * L;
+  float2 v[V];
+#pragma unroll
+  for (int i = 0; i < V; ++i) v[i] = line[fpad(lane + 32 * i)];
+  __syncwarp();
+  warp_fft<V>(v, line, tws, lane);
+#pragma unroll
+  for (int i = 0; i < V; ++i) line[fpad(lane + 32 * i)] = v[i];
+  __syncthreads();
+  if (l < valid) {
+#pragma unroll 4
+    for (uint32_t i = i0; i < N; i += ISTEP) g[l + i * p.estride] = tile[l * L + fpad(i)];
   }
 }
 
@@ -524,44 +713,42 @@ struct BuildZParams {
   BuildParams b;      // morphology, constants, window, mean, mode
   FftAxis az;         // z-axis plan (n = nz)
   uint32_t tx;        // columns per block
+  uint32_t stage;     // warp form: stage the morphology tile in shared memory
   uint32_t zlo, kz;   // kept shifted planes
   float2 *out;        // [nvol][kz][ny][nx]
 };
 
 __device__ __forceinline__ uint32_t igor(uint32_t j, uint32_t n);
 
-template <int MORPH>
+template <int MORPH, bool CONV>
 __global__ void __launch_bounds__(kFftThreads, 2) k_build_fft_z(BuildZParams p, const MaterialConsts *__restrict__ mcp) {
+  if (MORPH == 0 && conv_selected(p.b) != CONV) return;
   extern __shared__ float2 smem[];
   __shared__ MaterialConsts mc;
   load_consts(mc, mcp);
   const BuildParams &b = p.b;
   const uint32_t nz = p.az.n, TX = p.tx, S = TX + 1, nvol = b.nvol;
-  const size_t vsz = size_t(nz) * S;
-  float2 *bufa = smem, *bufb = smem + nvol * vsz;
+  const uint32_t vsz = nz * S;
+  float2 *bufa = smem, *bufb = smem + nvol * vsz, *tws = smem + 2 * nvol * vsz;
   const uint32_t nxt = (b.nx + TX - 1) / TX;
   const uint32_t xt = blockIdx.x % nxt, y = blockIdx.x / nxt, x0 = xt * TX;
-  const bool use_conv = MORPH == 0 && b.conv && *b.neg == 0u;
   __syncthreads();
   for (uint32_t t = threadIdx.x; t < TX * nz; t += blockDim.x) {
     const uint32_t l = t % TX, z = t / TX, x = x0 + l;
     float2 v[6];
     if (x < b.nx) {
-      const size_t i = (size_t(z) * b.ny + y) * b.nx + x;
-      if (use_conv)
-        voxel_values<MORPH, true>(b, mc, i, x, y, z, v);
-      else
-        voxel_values<MORPH, false>(b, mc, i, x, y, z, v);
+      voxel_values<MORPH, CONV>(b, mc, (size_t(z) * b.ny + y) * b.nx + x, x, y, z, v);
     } else {
 #pragma unroll
       for (int c = 0; c < 6; ++c) v[c] = make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int c = 0; c < 6; ++c)
-      if (uint32_t(c) < nvol) bufa[c * vsz + size_t(z) * S + l] = v[c];
+      if (uint32_t(c) < nvol) bufa[c * vsz + z * S + l] = v[c];
   }
+  stage_twiddles(tws, p.az.tw, nz);
   __syncthreads();
-  const float2 *res = stockham(bufa, bufb, p.az, TX, S, nvol);
+  const float2 *res = stockham(bufa, bufb, p.az, tws, TX, S, nvol);
   const size_t plane = size_t(b.nx) * b.ny;
   for (uint32_t t = threadIdx.x; t < nvol * p.kz * TX; t += blockDim.x) {
     const uint32_t l = t % TX, rest = t / TX;
@@ -569,7 +756,86 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_build_fft_z(BuildZParams p, 
     const uint32_t x = x0 + l;
     if (x >= b.nx) continue;
     const uint32_t u = igor(p.zlo + q, nz);
-    p.out[(size_t(v) * p.kz + q) * plane + size_t(y) * b.nx + x] = res[(size_t(v) * nz + u) * S + l];
+    p.out[(size_t(v) * p.kz + q) * plane + size_t(y) * b.nx + x] = res[(v * nz + u) * S + l];
+  }
+}
+
+// Warp-FFT form of k_build_fft_z for nz = 32 V (128, 256, 512): the block
+// builds the nvol x TX z-lines of its TX columns into padded shared lines,
+// each warp transforms whole lines in registers (no block barrier inside the
+// transform), and the kept planes are stored in rows of TX columns.
+template <int MORPH, bool CONV, int V, int TX>
+__global__ void __launch_bounds__(256) k_build_fft_z_warp(BuildZParams p, const MaterialConsts *__restrict__ mcp) {
+  if (MORPH == 0 && conv_selected(p.b) != CONV) return;
+  constexpr uint32_t NZ = 32 * V, L = line_stride(NZ, TX);
+  extern __shared__ float2 smem[];
+  __shared__ MaterialConsts mc;
+  load_consts(mc, mcp);
+  const BuildParams &b = p.b;
+  const uint32_t nvol = b.nvol;
+  float2 *tws = smem, *lines = smem + NZ;
+  const uint32_t nxt = (b.nx + TX - 1) / TX;
+  const uint32_t xt = blockIdx.x % nxt, y = blockIdx.x / nxt, x0 = xt * TX;
+  for (uint32_t t = threadIdx.x; t < NZ; t += blockDim.x) tws[t] = __ldg(&p.az.tw[t]);
+  // With p.stage the block's morphology tile [m][z][TX] is copied into shared
+  // memory with 16-byte cp.async first, so all of its loads are in flight at once.
+  const uint32_t nl = nvol * TX * L;
+  float4 *tile = reinterpret_cast<float4 *>(lines + nl + (nl & 1));
+  const float4 *src = CONV ? b.conv : b.vox;
+  const uint32_t l = threadIdx.x % TX, z0 = threadIdx.x / TX;
+  constexpr uint32_t ZSTEP = 256 / TX;
+  const uint32_t x = x0 + l;
+  const bool xin = x < b.nx;
+  const size_t plane = size_t(b.nx) * b.ny;
+  const float4 *col = src + size_t(y) * b.nx + x;  // material 0, z = 0 of this column
+  if (p.stage) {
+    if (xin)
+      for (uint32_t m = 0; m < b.nmat; ++m)
+        for (uint32_t z = z0; z < NZ; z += ZSTEP) {
+          const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(&tile[(m * NZ + z) * TX + l]));
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(col + m * b.nvox + z * plane)
+                       : "memory");
+        }
+    cp_async_wait_all();
+  }
+  __syncthreads();
+  for (uint32_t z = z0; z < NZ; z += ZSTEP) {
+    float2 v[6];
+    if (xin) {
+      float2 nt[6];
+      if (p.stage)
+        nt_entries_at<MORPH, CONV>(b, mc, tile + z * TX + l, size_t(NZ) * TX, nt);
+      else
+        nt_entries_at<MORPH, CONV>(b, mc, col + z * plane, b.nvox, nt);
+      values_from_nt(b, nt, x, y, z, v);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) v[c] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+      if (uint32_t(c) < nvol) lines[(c * TX + l) * L + fpad(z)] = v[c];
+  }
+  __syncthreads();
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (uint32_t li = warp; li < nvol * TX; li += nwarps) {
+    float2 *line = lines + li * L;
+    float2 v[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) v[i] = line[fpad(lane + 32 * i)];
+    __syncwarp();
+    warp_fft<V>(v, line, tws, lane);
+#pragma unroll
+    for (int i = 0; i < V; ++i) line[fpad(lane + 32 * i)] = v[i];
+    __syncwarp();
+  }
+  __syncthreads();
+  if (!xin) return;
+  float2 *out = p.out + size_t(y) * b.nx + x;
+  for (uint32_t c = 0; c < nvol; ++c) {
+    const float2 *ln = lines + (c * TX + l) * L;
+    float2 *oc = out + size_t(c) * p.kz * plane;
+    for (uint32_t q = z0; q < p.kz; q += ZSTEP) oc[q * plane] = ln[fpad(igor(p.zlo + q, NZ))];
   }
 }
 

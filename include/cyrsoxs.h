@@ -127,6 +127,12 @@ CYR_API int cyr_plan_info(const cyr_options *opt, uint32_t *info, uint32_t n);
  */
 CYR_API int cyr_device_errors(uint32_t *count);
 
+/*
+ * The launch configurations the engine's autotuner chose on this device, one
+ * line per shape ("kernel[shape]: choice time"), written into buf.
+ */
+CYR_API int cyr_tuning_report(char *buf, size_t len);
+
 /* Releases the library's cached scratch space on the current device. */
 CYR_API int cyr_release_scratch(void);
 
@@ -172,11 +178,13 @@ CYR_API int cyr_warp_affine_device(const float *d_src, float *d_dst, int width, 
  * kernel the engine launches is bracketed by a pair of CUDA events recorded
  * on its launch stream (no synchronisation is added).  cyr_profile_end waits
  * for the recorded events and returns, per kernel kind (cyr_stage_name), the
- * number of launches and their summed duration in milliseconds.  Launches
- * beyond max_launches are counted in *dropped and not timed.
+ * number of kernel launches, the number of timed calls (a call may launch a
+ * matched pair of kernels of which one returns at entry) and their summed
+ * duration in milliseconds.  Calls beyond max_launches are counted in
+ * *dropped and not timed.
  */
 CYR_API int cyr_profile_begin(uint32_t max_launches);
-CYR_API int cyr_profile_end(uint32_t *launches, double *ms, uint32_t nstages, uint32_t *dropped);
+CYR_API int cyr_profile_end(uint32_t *launches, uint32_t *calls, double *ms, uint32_t nstages, uint32_t *dropped);
 CYR_API const char *cyr_stage_name(uint32_t stage);
 CYR_API uint32_t cyr_num_stages(void);
 
