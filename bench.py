@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="headline", choices=["headline", "c2", "c1", "small"])
     ap.add_argument("--energies-per-step", type=int, default=ENERGIES_PER_STEP)
+    ap.add_argument("--strategy", type=int, default=0, choices=[0, 1, 2],
+                    help="0 auto, 1 per-energy spectra, 2 field spectra once per request")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--skip-cpu", action="store_true")
     return ap.parse_args()
@@ -151,11 +153,27 @@ def load_traffic(workload):
         return {}
 
 
-def algorithmic_bytes(kernel, w, nvol, nang, planes):
+def algorithmic_bytes(kernel, w, nvol, nang, planes, batch=1, npk=0):
     """Compulsory bytes per launch (each distinct element read once, written once).
 
-    planes = z planes kept after the fused build + z FFT (nz when not pruned)."""
+    planes = z planes kept after the fused build + z FFT (nz when not pruned); for the FIELDS
+    strategy nvol = packed field volumes, batch = energies per Ewald/rotation launch."""
     V, P, M = w.nvox, w.nx * w.ny, w.num_material
+    if npk:
+        table = {
+            "k_build_fields": (16 * M + 8 * npk) * V,
+            "k_moments": 16 * M * V,
+            "k_fft_pass<x>": 2 * 8 * npk * V,
+            "k_fft_pass<y>": 2 * 8 * npk * V,
+            "k_fft_pass<z>": 2 * 8 * npk * V,
+            # two planes of Z_j(k) and Z_j(-k) per pixel and energy, images out
+            "k_ewald_fields": batch * (4 * 8 * npk * P + 4 * nang * P),
+            "k_rotate_average": batch * (4 * nang * P + 4 * P),
+            "k_fill": batch * 4 * P,
+            "k_warp": batch * 8 * P,
+            "k_dc": 6 * 8 * npk,
+        }
+        return table.get(kernel)
     table = {
         "k_build": (16 * M + 8 * nvol) * V,
         "k_build_fft_z": 16 * M * V + 8 * nvol * planes * P,
@@ -248,7 +266,7 @@ def main():
     vox = workloads.voxels_torch(w).contiguous()
     opts = _native.Options(nx=w.nx, ny=w.ny, nz=w.nz, num_material=w.num_material, energies=energies,
                            start_angle=w.angles[0], end_angle=w.angles[1], increment_angle=w.angles[2],
-                           phys_size=w.phys_size, morphology_type=0)
+                           phys_size=w.phys_size, morphology_type=0, strategy=args.strategy)
     P = w.nx * w.ny
     out = torch.empty(len(energies) * P, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
@@ -299,16 +317,20 @@ def main():
     launches_per_step = sum(n for n, _, _ in kernels.values()) / prof_steps
     info = _native.plan_info(opts)
     nvol, planes = info["nvol"], info["planes"]
+    npk = info["packed_volumes"] if info["fields"] else 0
+    eb = info["energy_batch"]
+    batch = len(energies) / math.ceil(len(energies) / eb)  # mean energies per batched launch
+    ab = lambda k: algorithmic_bytes(k, w, nvol, nang, planes, batch, npk)  # noqa: E731
     dom = max(kernels.items(), key=lambda kv: kv[1][1])
     dom_name, (_, dom_ms, dom_n) = dom
     peak, peak_kind = load_peaks()
-    dom_bytes = algorithmic_bytes(dom_name, w, nvol, nang, planes)
+    dom_bytes = ab(dom_name)
     achieved = dom_bytes / (dom_ms / dom_n / 1000.0) / 1e9
     traffic = load_traffic(w.name).get(dom_name)
     # a "call" is one timed launch of the kernel's work (for Euler input the build kernels are
     # launched as a converted/trigonometric pair of which one returns at entry)
     kernel_table = {k: {"launches_per_step": n / prof_steps, "calls_per_step": c / prof_steps, "ms_per_call": ms / c,
-                        "gbs": (algorithmic_bytes(k, w, nvol, nang, planes) or 0) / (ms / c / 1000.0) / 1e9}
+                        "gbs": (ab(k) or 0) / (ms / c / 1000.0) / 1e9}
                     for k, (n, ms, c) in kernels.items()}
 
     result = {
@@ -368,7 +390,8 @@ def main():
         oracle.build()
         two = (w.angles[0], w.angles[0] + w.angles[2], w.angles[2])
         o2 = _native.Options(nx=w.nx, ny=w.ny, nz=w.nz, num_material=w.num_material, energies=energies[:1],
-                             start_angle=two[0], end_angle=two[1], increment_angle=two[2], phys_size=w.phys_size)
+                             start_angle=two[0], end_angle=two[1], increment_angle=two[2], phys_size=w.phys_size,
+                             strategy=2 if info["fields"] else 1)  # the strategy that was timed
         gpu2 = _native.cuda_main(o2, optical[:1], host_vox_np).astype(np.float64)
         ref2, secs = oracle.run_arrays(nx=w.nx, ny=w.ny, nz=w.nz, energies=energies[:1], optical=optical[:1],
                                        voxels=host_vox_np, angles=two, phys_size=w.phys_size)

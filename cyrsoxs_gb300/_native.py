@@ -40,6 +40,7 @@ class CyrOptions(ctypes.Structure):
         ("max_streams", ctypes.c_uint32),
         ("rot_mask", ctypes.c_uint32),
         ("reference_frame", ctypes.c_uint32),
+        ("strategy", ctypes.c_uint32),
     ]
 
 
@@ -109,7 +110,8 @@ class Options:
 
     def __init__(self, *, nx, ny, nz, num_material, energies, start_angle, end_angle, increment_angle, phys_size,
                  case_type=0, k_vectors=None, detector=(0.0, 0.0, 1.0), morphology_type=0, ewald_interpolation=1,
-                 windowing=0, scatter_approach=0, algorithm=0, max_streams=1, rot_mask=0, reference_frame=1):
+                 windowing=0, scatter_approach=0, algorithm=0, max_streams=1, rot_mask=0, reference_frame=1,
+                 strategy=0):
         self.energies = np.ascontiguousarray(energies, np.float32)
         kv = [[0.0, 0.0, 1.0]] if k_vectors is None else k_vectors
         self.k_vectors = np.ascontiguousarray(np.asarray(kv, np.float32).reshape(-1, 3))
@@ -132,6 +134,7 @@ class Options:
         s.max_streams = int(max_streams)
         s.rot_mask = int(rot_mask)
         s.reference_frame = int(reference_frame)
+        s.strategy = int(strategy)
         self.struct = s
 
     @property
@@ -195,10 +198,10 @@ def warp_affine_device(d_src: int, d_dst: int, width: int, height: int, coeffs, 
 
 
 def plan_info(opts: Options) -> dict:
-    info = (ctypes.c_uint32 * 6)()
-    check(lib().cyr_plan_info(opts.ref, info, 6))
+    info = (ctypes.c_uint32 * 9)()
+    check(lib().cyr_plan_info(opts.ref, info, 9))
     return {"nvol": info[0], "planes": info[1], "zlo": info[2], "pruned": bool(info[3]), "angles": info[4],
-            "k": info[5]}
+            "k": info[5], "fields": info[6], "packed_volumes": info[7], "energy_batch": info[8]}
 
 
 def tuning_report() -> str:

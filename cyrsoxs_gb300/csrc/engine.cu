@@ -16,6 +16,13 @@
 //   k_build -> k_fft_pass<x,y,z> -> k_dc -> per k: k_ewald_angles ->
 //   k_rotate_average -> k_fill + k_warp (detector) -> projection[e][k]
 //
+// FIELDS strategy (fields.cuh): the spectra of the 7 M + 1 energy independent
+// morphology fields are formed once per request; every energy and angle is
+// combined from them inside the Ewald kernel, batched over energies:
+//
+//   k_moments -> k_field_means -> k_build_fields -> 3D FFT -> k_dc -> per k and
+//   energy batch: k_ewald_fields -> k_rotate_average -> k_fill + k_warp
+//
 // All per-request constants (optical constants of every energy, angle
 // coefficients, warp coefficients, q-grid and window tables) are computed on
 // the host in double and uploaded once, before any kernel of the request.
@@ -38,6 +45,7 @@
 #include "../../include/cyrsoxs.h"
 #include "geometry.h"
 #include "kernels.cuh"
+#include "fields.cuh"
 
 namespace cyr {
 namespace {
@@ -121,10 +129,14 @@ struct DeviceBuffer {
 
 // Optional per-launch timing: an event pair around every kernel launch,
 // read back after the caller has synchronised (cyr_profile_end).
-enum Stage { kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kBuildZ, kNumStages };
+enum Stage {
+  kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kBuildZ,
+  kFieldMeans, kBuildFields, kEwaldFields, kNumStages
+};
 const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_pass<y>", "k_fft_pass<z>", "k_dc",
                                              "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp",
-                                             "k_moments", "k_entry_means", "k_build_fft_z"};
+                                             "k_moments", "k_entry_means", "k_build_fft_z",
+                                             "k_field_means", "k_build_fields", "k_ewald_fields"};
 
 struct Profiler {
   bool active = false;
@@ -163,7 +175,7 @@ struct DeviceContext {
   std::mutex mu;
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
-  DeviceBuffer spec, images, avg, params, dc, vox_in, out_in, moments, means, errors, conv, flags;
+  DeviceBuffer spec, images, avg, params, dc, vox_in, out_in, moments, means, errors, conv, flags, fmean;
   cudaEvent_t last_use = nullptr;  // completion of the last request that used the scratch
 };
 
@@ -351,7 +363,18 @@ struct Plan {
   std::vector<ZTune> zcands;            // autotuning candidates of the warp form
   size_t vstride = 0;                   // elements per spectrum volume
   uint32_t p0 = 0, p1 = 0, pn = 0;      // planes of unshifted z bins 0, 1, nz-1
+  // FIELDS strategy
+  bool fields = false;
+  uint32_t npk = 0;                     // packed field volumes
+  uint32_t ebatch = 1;                  // energies per Ewald / rotation launch
+  size_t off_fcoef = 0, off_kmag = 0, off_mat = 0;
 };
+
+// Device bytes of the FIELDS strategy: packed field spectra, per-batch images and averages.
+size_t field_bytes(const Plan &pl) {
+  return size_t(pl.npk) * pl.nvox * sizeof(float2) + size_t(pl.ebatch) * (pl.nang + 1) * pl.npix * sizeof(float) +
+         pl.arena.size() + (num_fields(pl.nmat) + 2 * pl.npk) * sizeof(float2);
+}
 
 // Dynamic shared memory of k_build_fft_z_warp: twiddles, lines, optional tile.
 inline size_t zwarp_smem(uint32_t nz, uint32_t nvol, uint32_t tx, uint32_t nmat, bool stage) {
@@ -431,7 +454,7 @@ int validate(const cyr_options *o) {
   if (o->case_type > 2) return fail(CYR_ERR_ARGUMENT, "case_type must be 0, 1 or 2");
   if (o->case_type != 0 && (o->num_k < 1 || !o->k_vectors)) return fail(CYR_ERR_ARGUMENT, "k vectors missing");
   if (o->morphology_type > 1 || o->ewald_interpolation > 1 || o->windowing > 1 || o->scatter_approach > 1 ||
-      o->algorithm > 1 || o->reference_frame > 1)
+      o->algorithm > 1 || o->reference_frame > 1 || o->strategy > 2)
     return fail(CYR_ERR_ARGUMENT, "enumerated option out of range");
   if (o->start_angle > o->end_angle) return fail(CYR_ERR_ARGUMENT, "start angle greater than end angle");
   if (!near_equal(o->start_angle, o->end_angle) && near_equal(o->increment_angle, 0.f))
@@ -532,6 +555,7 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
   }
   // material constants per energy, in double, scaled by 1/4pi (uniaxial.h:155-162)
   std::vector<MaterialConsts> mcs(pl.ne);
+  std::vector<std::complex<double>> cA(size_t(pl.ne) * pl.nmat), cB(cA.size()), cC(cA.size()), cD(cA.size());
   const double s = 1.0 / (4.0 * kPi);
   for (uint32_t e = 0; e < pl.ne; ++e) {
     MaterialConsts &mc = mcs[e];
@@ -549,6 +573,8 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
       mc.B[m] = make_float2(float(B.real() * s), float(B.imag() * s));
       mc.C[m] = make_float2(float(C.real() * s), float(C.imag() * s));
       mc.D[m] = make_float2(float(D.real() * s), float(D.imag() * s));
+      const size_t em = size_t(e) * pl.nmat + m;
+      cA[em] = A * s, cB[em] = B * s, cC[em] = C * s, cD[em] = D * s;
     }
   }
   pl.arena.clear();
@@ -598,11 +624,90 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
   pl.off_hx = arena_put(pl.arena, hx.data(), hx.size());
   pl.off_hy = arena_put(pl.arena, hy.data(), hy.size());
   pl.off_hz = arena_put(pl.arena, hz.data(), hz.size());
+
+  // FIELDS strategy: choose it, then its tables
+  pl.npk = num_packed(pl.nmat);
+  if (o->strategy == CYR_STRATEGY_AUTO) {
+    // plane-volumes moved per request (read + write of the FFT passes, morphology reads)
+    const double planes = pl.pruned ? pl.kz : pl.nz;
+    const double spectra = pl.material_frame ? double(pl.nk) * pl.nang * 3.0 : double(pl.nvol);
+    const double per_energy = double(pl.ne) * (spectra * planes + 2.0 * pl.nmat * pl.nz);
+    const double once = (1.5 * pl.npk + 2.0 * pl.nmat) * pl.nz;
+    pl.fields = once < per_energy;
+  } else {
+    pl.fields = o->strategy == CYR_STRATEGY_FIELDS;
+  }
+  {
+    const size_t img = size_t(pl.nang) * pl.npix * sizeof(float);
+    pl.ebatch = uint32_t(std::max<size_t>(1, std::min<size_t>(pl.ne, (size_t(96) << 20) / img)));
+  }
+  if (pl.fields) {
+    // coef[e][v][j] = (alpha, beta): Nt_v(k) = sum_j alpha Z_j(k) + beta conj Z_j(-k), where
+    // Z_j = F_2j + i F_2j+1 and field g = 7 m + f (f: u_x^2 u_y^2 u_z^2 u_xu_y u_xu_z u_yu_z phi_ui), T last
+    const uint32_t nf = num_fields(pl.nmat), npk = pl.npk;
+    std::vector<float4> fc(size_t(pl.ne) * 6 * npk);
+    std::vector<std::complex<double>> c(size_t(6) * 2 * npk);
+    for (uint32_t e = 0; e < pl.ne; ++e) {
+      std::fill(c.begin(), c.end(), std::complex<double>(0.0, 0.0));
+      auto at = [&](int v, uint32_t g) -> std::complex<double> & { return c[size_t(v) * 2 * npk + g]; };
+      std::complex<double> R(0.0, 0.0);  // common part of the diagonal coefficients
+      for (uint32_t m = 0; m < pl.nmat; ++m) R += cB[size_t(e) * pl.nmat + m] + cC[size_t(e) * pl.nmat + m];
+      R /= double(2 * pl.nmat);
+      for (uint32_t m = 0; m < pl.nmat; ++m) {
+        const size_t em = size_t(e) * pl.nmat + m;
+        const uint32_t g = kFieldsPerMaterial * m;
+        const std::complex<double> B = cB[em] - R, C = cC[em] - R, DB = cD[em] + cB[em] - R;
+        const int diag[3] = {0, 3, 5};  // xx yy zz
+        for (int i = 0; i < 3; ++i) {
+          for (int f = 0; f < 3; ++f) at(diag[i], g + f) = f == i ? DB : B;
+          at(diag[i], g + 6) = C;
+        }
+        at(1, g + 3) = cD[em];  // xy
+        at(2, g + 4) = cD[em];  // xz
+        at(4, g + 5) = cD[em];  // yz
+      }
+      for (int i : {0, 3, 5}) at(i, nf - 1) = R;
+      const std::complex<double> I(0.0, 1.0);
+      for (int v = 0; v < 6; ++v)
+        for (uint32_t j = 0; j < npk; ++j) {
+          const std::complex<double> ca = at(v, 2 * j), cb = at(v, 2 * j + 1);
+          const std::complex<double> al = 0.5 * (ca - I * cb), be = 0.5 * (ca + I * cb);
+          fc[(size_t(e) * 6 + v) * npk + j] =
+              make_float4(float(al.real()), float(al.imag()), float(be.real()), float(be.imag()));
+        }
+    }
+    pl.off_fcoef = arena_put(pl.arena, fc.data(), fc.size());
+    std::vector<float> km(pl.ne);
+    for (uint32_t e = 0; e < pl.ne; ++e) {
+      const float wavelength = static_cast<float>(1239.84197 / o->energies[e]);  // src/cudaMain.cu:607-608
+      km[e] = static_cast<float>(2 * kPi / wavelength);
+    }
+    pl.off_kmag = arena_put(pl.arena, km.data(), km.size());
+    // per (k, angle): p_c = sum_v M[c][v] Nt_v.  LAB: p = Nt E.  MATERIAL: p = R^T Nt E.
+    const uint32_t sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    std::vector<float> mat(size_t(pl.nk) * pl.nang * 18, 0.f);
+    for (size_t ka = 0; ka < size_t(pl.nk) * pl.nang; ++ka) {
+      double M[3][6] = {};
+      const float *E = &pl.evec[ka * 3];
+      for (int cc = 0; cc < 3; ++cc)
+        for (int b = 0; b < 3; ++b) {
+          if (pl.material_frame) {
+            for (int i = 0; i < 3; ++i) M[cc][sym[i][b]] += double(pl.rmats[ka].m[i * 3 + cc]) * double(E[b]);
+          } else {
+            M[cc][sym[cc][b]] += double(E[b]);
+          }
+        }
+      for (int cc = 0; cc < 3; ++cc)
+        for (int v = 0; v < 6; ++v) mat[ka * 18 + cc * 6 + v] = float(M[cc][v]);
+    }
+    pl.off_mat = arena_put(pl.arena, mat.data(), mat.size());
+  }
   pl.arena.resize((pl.arena.size() + 255) & ~size_t(255));
   return CYR_OK;
 }
 
 size_t request_bytes(const Plan &pl) {
+  if (pl.fields) return field_bytes(pl) + pl.nmat * kMoments * sizeof(double) + 64 * sizeof(float2);
   return pl.nvol * pl.vstride * sizeof(float2) + (pl.euler ? pl.nvox * pl.nmat * sizeof(float4) : 0) + size_t(pl.nang) * pl.npix * sizeof(float) + pl.npix * sizeof(float) +
          pl.arena.size() + 64 * sizeof(float2);
 }
@@ -640,19 +745,133 @@ EwaldParams ewald_params(const Plan &pl, const cyr_options *o, const unsigned ch
   return p;
 }
 
+// FIELDS strategy after the moments: field means, packed field spectra, then
+// every energy (in batches) and k from them.
+int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const unsigned char *dp,
+               const float4 *d_vox, float *d_out, cudaStream_t st) {
+  const uint32_t nf = num_fields(pl.nmat), npk = pl.npk;
+  CYR_TRY(ctx.fmean.ensure(nf * sizeof(float)));
+  CYR_TRY(ctx.spec.ensure(size_t(npk) * pl.nvox * sizeof(float2)));
+  CYR_TRY(ctx.dc.ensure(size_t(npk) * sizeof(float2)));
+  CYR_TRY(ctx.images.ensure(size_t(pl.ebatch) * pl.nang * pl.npix * sizeof(float)));
+  CYR_TRY(ctx.avg.ensure(size_t(pl.ebatch) * pl.npix * sizeof(float)));
+  float2 *spec = ctx.spec.as<float2>();
+  int slot = ctx.prof.begin(kFieldMeans, st);
+  k_field_means<<<1, 128, 0, st>>>(ctx.moments.as<double>(), pl.nmat, pl.nvox, ctx.fmean.as<float>());
+  ctx.prof.end(slot, st);
+  CYR_CUDA(cudaGetLastError());
+  FieldParams fp{};
+  fp.vox = d_vox;
+  fp.nx = pl.nx, fp.ny = pl.ny, fp.nz = pl.nz, fp.nmat = pl.nmat;
+  fp.nvox = pl.nvox;
+  fp.mean = ctx.fmean.as<float>();
+  if (pl.hanning) {
+    fp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
+    fp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
+    fp.hann_z = reinterpret_cast<const float *>(dp + pl.off_hz);
+  }
+  fp.out = spec;
+  int sms = 0;
+  CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  const uint32_t blocks = uint32_t(std::min<size_t>((pl.nvox + 255) / 256, size_t(sms) * 8));
+  slot = ctx.prof.begin(kBuildFields, st);
+  if (o->morphology_type == 0)
+    k_build_fields<0><<<blocks, 256, 0, st>>>(fp);
+  else
+    k_build_fields<1><<<blocks, 256, 0, st>>>(fp);
+  ctx.prof.end(slot, st);
+  CYR_CUDA(cudaGetLastError());
+  CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st));
+  slot = ctx.prof.begin(kDc, st);
+  k_dc<<<1, (npk + 31) / 32 * 32, 0, st>>>(spec, npk, pl.nvox, pl.nx, pl.ny, pl.nz, 0, 1 % pl.nz, pl.nz - 1,
+                                           ctx.dc.as<float2>());
+  ctx.prof.end(slot, st);
+  CYR_CUDA(cudaGetLastError());
+
+  FieldEwaldParams fe{};
+  fe.zspec = spec;
+  fe.zdc = ctx.dc.as<float2>();
+  fe.npk = npk;
+  fe.nvox = pl.nvox;
+  fe.coef = reinterpret_cast<const float4 *>(dp + pl.off_fcoef);
+  fe.kmag = reinterpret_cast<const float *>(dp + pl.off_kmag);
+  fe.g.start = -static_cast<float>(kPi / o->phys_size);
+  fe.g.dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nx - 1) * 1.0));
+  fe.g.dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.ny - 1) * 1.0));
+  fe.g.dz = pl.twod ? 0.f : static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nz - 1) * 1.0));
+  fe.g.nx = pl.nx, fe.g.ny = pl.ny, fe.g.nz = pl.nz;
+  fe.g.interp = o->ewald_interpolation;
+  fe.g.twod = pl.twod ? 1u : 0u;
+  fe.qx = reinterpret_cast<const float *>(dp + pl.off_qx);
+  fe.qy = reinterpret_cast<const float *>(dp + pl.off_qy);
+  fe.qz = reinterpret_cast<const float *>(dp + pl.off_qz);
+  fe.nangles = pl.nang;
+  fe.images = ctx.images.as<float>();
+  const size_t fsmem = size_t(6) * npk * sizeof(float4);
+  const unsigned pix_blocks = unsigned((pl.npix + 255) / 256);
+  const unsigned fpix_blocks = unsigned((pl.npix + kFieldEwaldThreads - 1) / kFieldEwaldThreads);
+  const int W = int(pl.ny), H = int(pl.nx);  // the reference hands NPP width = Ny, height = Nx
+  const WarpCoef *dwarp = reinterpret_cast<const WarpCoef *>(dp + pl.off_warp);
+  const float *dmat = reinterpret_cast<const float *>(dp + pl.off_mat);
+  const float fillv = o->rot_mask ? 0.f : std::numeric_limits<float>::quiet_NaN();
+  const size_t ostride = size_t(pl.nk) * pl.npix;
+  for (uint32_t k = 0; k < pl.nk; ++k) {
+    const KFrame &f = pl.frames[k];
+    fe.kvx = f.k.x, fe.kvy = f.k.y, fe.kvz = f.k.z;
+    fe.mat = dmat + size_t(k) * pl.nang * 18;
+    RotateParams rp{};
+    rp.images = ctx.images.as<float>();
+    rp.coef = dwarp + size_t(k) * pl.nang;
+    rp.W = W, rp.H = H;
+    rp.nangles = pl.nang;
+    rp.rot_mask = o->rot_mask;
+    rp.avg = ctx.avg.as<float>();
+    for (uint32_t e0 = 0; e0 < pl.ne; e0 += pl.ebatch) {
+      const uint32_t nb = std::min(pl.ebatch, pl.ne - e0);
+      fe.e0 = e0;
+      slot = ctx.prof.begin(kEwaldFields, st);
+      k_ewald_fields<<<dim3(fpix_blocks, nb), kFieldEwaldThreads, fsmem, st>>>(fe);
+      ctx.prof.end(slot, st);
+      slot = ctx.prof.begin(kRotate, st);
+      k_rotate_average<<<dim3(pix_blocks, nb), 256, 0, st>>>(rp);
+      ctx.prof.end(slot, st);
+      float *dst = d_out + (size_t(e0) * pl.nk + k) * pl.npix;
+      slot = ctx.prof.begin(kFill, st);
+      k_fill<<<dim3(pix_blocks, nb), 256, 0, st>>>(dst, pl.npix, fillv, ostride);
+      ctx.prof.end(slot, st);
+      slot = ctx.prof.begin(kWarp, st);
+      k_warp<<<dim3(pix_blocks, nb), 256, 0, st>>>(ctx.avg.as<float>(), dst, W, H, pl.detector_warp[k], pl.npix,
+                                                   ostride);
+      ctx.prof.end(slot, st);
+      CYR_CUDA(cudaGetLastError());
+    }
+  }
+  CYR_CUDA(cudaEventRecord(ctx.last_use, st));
+  return CYR_OK;
+}
+
 int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, const float4 *d_vox, float *d_out,
                 cudaStream_t st) {
   Plan pl;
   CYR_TRY(make_plan(o, optical, pl));
   CYR_TRY(setup_attrs(ctx));
+  if (pl.fields && o->strategy == CYR_STRATEGY_AUTO) {
+    // AUTO falls back to the per-energy spectra when the field volumes do not fit
+    size_t free_b = 0, total_b = 0;
+    CYR_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t reusable = ctx.spec.bytes + ctx.images.bytes + ctx.avg.bytes;
+    if (field_bytes(pl) + (size_t(1) << 30) > free_b + reusable) pl.fields = false;
+  }
   // scratch (grow-only); wait for the previous user of the scratch
   CYR_CUDA(cudaStreamWaitEvent(st, ctx.last_use, 0));
-  CYR_TRY(ctx.spec.ensure(pl.nvol * pl.vstride * sizeof(float2)));
   CYR_TRY(ctx.errors.ensure(sizeof(unsigned)));
   CYR_CUDA(cudaMemsetAsync(ctx.errors.ptr, 0, sizeof(unsigned), st));
-  CYR_TRY(ctx.images.ensure(size_t(pl.nang) * pl.npix * sizeof(float)));
-  CYR_TRY(ctx.avg.ensure(pl.npix * sizeof(float)));
-  CYR_TRY(ctx.dc.ensure(8 * sizeof(float2)));
+  if (!pl.fields) {
+    CYR_TRY(ctx.spec.ensure(pl.nvol * pl.vstride * sizeof(float2)));
+    CYR_TRY(ctx.images.ensure(size_t(pl.nang) * pl.npix * sizeof(float)));
+    CYR_TRY(ctx.avg.ensure(pl.npix * sizeof(float)));
+    CYR_TRY(ctx.dc.ensure(8 * sizeof(float2)));
+  }
   CYR_TRY(ctx.params.ensure(pl.arena.size()));
   CYR_CUDA(cudaMemcpyAsync(ctx.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
   const unsigned char *dp = ctx.params.as<unsigned char>();
@@ -661,7 +880,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   CYR_TRY(ctx.means.ensure(size_t(pl.ne) * 6 * sizeof(float2)));
   CYR_CUDA(cudaMemsetAsync(ctx.moments.ptr, 0, size_t(pl.nmat) * kMoments * sizeof(double), st));
   // Euler morphologies are converted once per request to the trigonometry-free vector form
-  const bool convert = o->morphology_type == 0;
+  const bool convert = o->morphology_type == 0 && !pl.fields;
   CYR_TRY(ctx.flags.ensure(sizeof(unsigned)));
   CYR_CUDA(cudaMemsetAsync(ctx.flags.ptr, 0, sizeof(unsigned), st));
   if (convert) CYR_TRY(ctx.conv.ensure(pl.nvox * pl.nmat * sizeof(float4)));
@@ -688,6 +907,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       k_moments<1><<<grid, 256, 0, st>>>(mp);
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
+    if (pl.fields) return run_fields(ctx, o, pl, dp, d_vox, d_out, st);
     slot = ctx.prof.begin(kMeans, st);
     k_entry_means<<<1, 64, 0, st>>>(ctx.moments.as<double>(), pl.nmat, pl.nvox,
                                     reinterpret_cast<const MaterialConsts *>(dp + pl.off_mc), pl.ne,
@@ -948,8 +1168,9 @@ int cyr_plan_info(const cyr_options *opt, uint32_t *info, uint32_t n) {
   std::vector<float> dummy(size_t(opt->num_energies) * opt->num_material * 4, 0.f);
   Plan pl;
   CYR_TRY(make_plan(opt, dummy.data(), pl));
-  const uint32_t v[6] = {pl.nvol, pl.pruned ? pl.kz : pl.nz, pl.zlo, pl.pruned ? 1u : 0u, pl.nang, pl.nk};
-  for (uint32_t i = 0; i < n && i < 6; ++i) info[i] = v[i];
+  const uint32_t v[9] = {pl.nvol, pl.pruned ? pl.kz : pl.nz, pl.zlo, pl.pruned ? 1u : 0u, pl.nang, pl.nk,
+                         pl.fields ? 1u : 0u, pl.npk, pl.ebatch};
+  for (uint32_t i = 0; i < n && i < 9; ++i) info[i] = v[i];
   return CYR_OK;
 }
 
@@ -1000,6 +1221,7 @@ int cyr_release_scratch(void) {
   ctx->errors.release();
   ctx->conv.release();
   ctx->flags.release();
+  ctx->fmean.release();
   ctx->vox_in.release();
   ctx->out_in.release();
   return CYR_OK;

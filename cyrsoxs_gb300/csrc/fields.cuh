@@ -1,0 +1,203 @@
+// Field-spectrum form of the scattering path: the morphology's energy
+// independent fields are transformed once per request and every energy and
+// E angle is formed from them at the Ewald sample points.
+//
+// Per material m the uniaxial tensor of a voxel is (include/uniaxial.h:82-151)
+//   Nt_ij = A u_i^2 + B (|u|^2 - u_i^2) + C phi_ui      (i = j)
+//   Nt_ij = D u_i u_j                                    (i != j)
+// with u = sqrt(phi_a) s (phi_a s_i s_j = u_i u_j), so it is linear in the
+// seven real fields u_x^2, u_y^2, u_z^2, u_x u_y, u_x u_z, u_y u_z, phi_ui,
+// with energy dependent complex coefficients.  The FFT is linear, hence
+//   FFT(Nt_v) = sum_g c_vg(E) FFT(F_g),
+// exactly.  The diagonal coefficients share a common part R(E) (the base
+// optical constants are the same for every material), which would cancel in
+// the sum and amplify the FP32 rounding of the field spectra; it is taken out
+// with one more field, T = sum_m (|u_m|^2 + phi_ui_m):
+//   Nt_xx = sum_m [(D+B-R) u_x^2 + (B-R)(u_y^2 + u_z^2) + (C-R) phi_ui] + R T.
+// The 7 M + 1 real fields are packed in pairs into complex volumes
+// Z_j = F_2j + i F_2j+1 and transformed with the engine's complex 3D FFT; the
+// Ewald kernel unpacks them with
+//   F_2j(k) = (Z_j(k) + conj Z_j(-k)) / 2,  F_2j+1(k) = (Z_j(k) - conj Z_j(-k)) / 2i.
+// Every field is windowed and has its volume mean removed before the FFT,
+// which changes only bin 0; bin 0 is always replaced by the mean of its six
+// (four in 2D) neighbours (src/cudaMain.cu:123-176), a symmetric stencil, so
+// replacing it in each Z_j before unpacking is the same as replacing it in
+// each tensor entry.
+#pragma once
+
+namespace cyr {
+
+constexpr int kFieldsPerMaterial = 7;
+
+__host__ __device__ constexpr uint32_t num_fields(uint32_t nmat) { return kFieldsPerMaterial * nmat + 1; }
+__host__ __device__ constexpr uint32_t num_packed(uint32_t nmat) { return (num_fields(nmat) + 1) / 2; }
+
+// Field means from the per-material volume moments (k_moments), T last.
+__global__ void k_field_means(const double *__restrict__ mom, uint32_t nmat, size_t nvox, float *__restrict__ out) {
+  const uint32_t nf = num_fields(nmat);
+  for (uint32_t g = threadIdx.x; g < nf; g += blockDim.x) {
+    double v = 0.0;
+    if (g + 1 < nf) {
+      v = mom[(g / kFieldsPerMaterial) * kMoments + g % kFieldsPerMaterial];
+    } else {
+      for (uint32_t m = 0; m < nmat; ++m) {
+        const double *M = mom + m * kMoments;
+        v += M[0] + M[1] + M[2] + M[6];
+      }
+    }
+    out[g] = float(v / double(nvox));
+  }
+}
+
+struct FieldParams {
+  const float4 *vox;     // [nmat][nvox] as the reference stores Voxel::s1
+  uint32_t nx, ny, nz, nmat;
+  size_t nvox;
+  const float *mean;     // [num_fields] volume mean of each windowed field
+  const float *hann_x, *hann_y, *hann_z;  // null when no windowing
+  float2 *out;           // [num_packed][nvox]: field 2j in .x, field 2j+1 in .y
+};
+
+// Windowed, mean-free fields of every voxel, packed in pairs.
+template <int MORPH>
+__global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
+  const size_t stride = size_t(gridDim.x) * blockDim.x;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
+    float w = 1.f;
+    if (p.hann_x) {
+      const uint32_t x = uint32_t(i % p.nx), y = uint32_t((i / p.nx) % p.ny), z = uint32_t(i / (size_t(p.nx) * p.ny));
+      w = p.hann_x[x] * p.hann_y[y] * p.hann_z[z];
+    }
+    float T = 0.f, pend = 0.f;
+    uint32_t g = 0;
+    float2 *o = p.out + i;
+    // g is the same in every thread: the parity branches do not diverge
+    auto emit = [&](float v) {
+      v -= p.mean[g];
+      if (g & 1u)
+        o[size_t(g >> 1) * p.nvox] = make_float2(pend, v);
+      else
+        pend = v;
+      ++g;
+    };
+    for (uint32_t m = 0; m < p.nmat; ++m) {
+      float sx, sy, sz, pa, pui;
+      director<MORPH>(__ldg(&p.vox[m * p.nvox + i]), sx, sy, sz, pa, pui);
+      const float wa = w * pa;
+      const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
+      T += f0 + f1 + f2 + f6;
+      emit(f0);
+      emit(f1);
+      emit(f2);
+      emit(wa * sx * sy);
+      emit(wa * sx * sz);
+      emit(wa * sy * sz);
+      emit(f6);
+    }
+    emit(T);
+    if (g & 1u) o[size_t(g >> 1) * p.nvox] = make_float2(pend, 0.f);
+  }
+}
+
+// Ewald projection from the packed field spectra, for a batch of energies
+// (blockIdx.y) and every E angle.  Per energy the unpacking and combination
+// coefficients of tensor entry v (xx xy xz yy yz zz) and packed volume j are
+// coef[e][v][j] = (alpha, beta):  Nt_v(k) = sum_j alpha Z_j(k) + beta conj Z_j(-k).
+// Per angle a, the scattered polarization is p_c = sum_v M[a][c][v] Nt_v with
+// a real 3 x 6 matrix (LAB frame: E_b on entry (c, b); MATERIAL frame: the
+// rotation R^T folded in, include/uniaxial.h:163-165).
+struct FieldEwaldParams {
+  const float2 *zspec;   // [npk][nz][ny][nx], unshifted (natural) bin order
+  const float2 *zdc;     // [npk] DC replacement of each packed volume
+  uint32_t npk;
+  size_t nvox;
+  const float4 *coef;    // [ne][6][npk]: (alpha.x, alpha.y, beta.x, beta.y)
+  const float *kmag;     // [ne]
+  uint32_t e0;           // first energy of this batch
+  float kvx, kvy, kvz;   // k vector
+  EwaldGeom g;           // kmag, kx, ky, kz filled per energy
+  const float *qx, *qy, *qz;
+  uint32_t nangles;
+  const float *mat;      // [nangles][3][6]
+  float *images;         // [batch][nangles][npix]
+};
+
+constexpr int kFieldEwaldThreads = 128;
+
+__global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldParams p) {
+  extern __shared__ float4 fcoef[];  // [6][npk]
+  const uint32_t eb = blockIdx.y, e = p.e0 + eb;
+  for (uint32_t t = threadIdx.x; t < 6 * p.npk; t += blockDim.x) fcoef[t] = p.coef[size_t(e) * 6 * p.npk + t];
+  __syncthreads();
+  const uint32_t nx = p.g.nx, ny = p.g.ny, nz = p.g.nz;
+  const size_t npix = size_t(nx) * ny;
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= npix) return;
+  const uint32_t Y = uint32_t(t / nx), X = uint32_t(t % nx);
+  EwaldGeom g = p.g;
+  g.kmag = p.kmag[e];
+  g.kx = __fmul_rn(g.kmag, p.kvx), g.ky = __fmul_rn(g.kmag, p.kvy), g.kz = __fmul_rn(g.kmag, p.kvz);
+  uint32_t zs[2];
+  float w1;
+  int nplanes;
+  float *img = p.images + size_t(eb) * p.nangles * npix + t;
+  if (!ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes)) {
+    const float nanv = __int_as_float(0x7fc00000);
+    for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
+    return;
+  }
+  const uint32_t ux = igor(X, nx), uy = igor(Y, ny);
+  const uint32_t mx = ux ? nx - ux : 0u, my = uy ? ny - uy : 0u;
+  float2 N[2][6];
+  float Q[2][3];
+  for (int pl = 0; pl < nplanes; ++pl) {
+    const uint32_t uz = g.twod ? 0u : igor(zs[pl], nz);
+    const uint32_t mz = uz ? nz - uz : 0u;
+    const bool is_dc = ux == 0 && uy == 0 && uz == 0;
+    const size_t i0 = size_t(ux) + size_t(uy) * nx + size_t(uz) * npix;
+    const size_t i1 = size_t(mx) + size_t(my) * nx + size_t(mz) * npix;
+#pragma unroll
+    for (int v = 0; v < 6; ++v) N[pl][v] = make_float2(0.f, 0.f);
+    const float2 *zj = p.zspec;
+#pragma unroll 2
+    for (uint32_t j = 0; j < p.npk; ++j, zj += p.nvox) {
+      float2 a, b;
+      if (is_dc) {
+        a = b = p.zdc[j];
+      } else {
+        a = __ldg(&zj[i0]);
+        b = __ldg(&zj[i1]);
+      }
+      b.y = -b.y;  // conj Z_j(-k)
+#pragma unroll
+      for (int v = 0; v < 6; ++v) {
+        const float4 c = fcoef[v * p.npk + j];
+        N[pl][v].x += c.x * a.x - c.y * a.y + c.z * b.x - c.w * b.y;
+        N[pl][v].y += c.x * a.y + c.y * a.x + c.z * b.y + c.w * b.x;
+      }
+    }
+    Q[pl][0] = g.kx + p.qx[X];
+    Q[pl][1] = g.ky + p.qy[Y];
+    Q[pl][2] = g.kz + (g.twod ? 0.f : p.qz[zs[pl]]);
+  }
+  const float d = g.kmag * g.kmag;
+  const float w0 = 1.f - w1;
+  for (uint32_t a = 0; a < p.nangles; ++a) {
+    const float *M = p.mat + size_t(a) * 18;
+    float I[2];
+    for (int pl = 0; pl < nplanes; ++pl) {
+      float2 pc[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int v = 0; v < 6; ++v) acc = cfma(__ldg(&M[c * 6 + v]), N[pl][v], acc);
+        pc[c] = acc;
+      }
+      I[pl] = intensity(Q[pl][0], Q[pl][1], Q[pl][2], d, pc[0], pc[1], pc[2]);
+    }
+    img[size_t(a) * npix] = nplanes == 2 ? w0 * I[0] + w1 * I[1] : I[0];
+  }
+}
+
+}  // namespace cyr

@@ -916,42 +916,58 @@ __device__ __forceinline__ float intensity(float Q0, float Q1, float Q2, float d
   return t0.x * t0.x + t0.y * t0.y + t1.x * t1.x + t1.y * t1.y + t2.x * t2.x + t2.y * t2.y;
 }
 
+// Where detector pixel (X, Y) meets the Ewald sphere: false for a NaN pixel,
+// else the plane(s) to read (shifted z indices Z0 [, Z1 = Z0 + 1 with weight
+// w1]).  Every operation is in float with correct rounding, in the
+// reference's order (include/uniaxial.h:720-760), so NaN masks agree exactly.
+struct EwaldGeom {
+  float start, dx, dy, dz;
+  float kmag, kx, ky, kz;
+  uint32_t nx, ny, nz;
+  uint32_t interp, twod;
+};
+
+__device__ __forceinline__ bool ewald_geometry(const EwaldGeom &g, uint32_t X, uint32_t Y, uint32_t &Z0, uint32_t &Z1,
+                                               float &w1, int &nplanes) {
+  const float posx = __fadd_rn(g.start, __fmul_rn(float(X), g.dx));
+  const float posy = __fadd_rn(g.start, __fmul_rn(float(Y), g.dy));
+  const float ax = __fadd_rn(g.kx, posx), ay = __fadd_rn(g.ky, posy);
+  const float val = __fsub_rn(__fsub_rn(__fmul_rn(g.kmag, g.kmag), __fmul_rn(ax, ax)), __fmul_rn(ay, ay));
+  Z0 = Z1 = 0;
+  w1 = 0.f;  // weight of plane Z1
+  nplanes = 1;
+  if ((val < 0.f) || (X == g.nx - 1) || (Y == g.ny - 1)) return false;
+  const float posz = __fadd_rn(-g.kz, __fsqrt_rn(val));
+  if (g.interp == 0) {
+    if (!g.twod) {
+      const float r = roundf(__fdiv_rn(__fsub_rn(posz, g.start), g.dz));  // round(), uniaxial.h:749
+      Z0 = r <= 0.f ? 0u : uint32_t(r);
+    }
+    if (Z0 > g.nz - 1) return false;
+  } else if (!g.twod) {
+    const float tz = __fdiv_rn(__fsub_rn(posz, g.start), g.dz);
+    Z0 = tz <= 0.f ? 0u : uint32_t(tz);
+    // Z > Nz-1 is the reference's NaN rule; Z == Nz-1 would read outside the volume
+    if (Z0 >= g.nz - 1) return false;
+    Z1 = Z0 + 1;
+    nplanes = 2;
+    const float base = __fadd_rn(g.start, __fmul_rn(float(Z0), g.dz));
+    w1 = __fdiv_rn(__fsub_rn(posz, base), g.dz);
+  }
+  return true;
+}
+
 __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
   const size_t npix = size_t(p.nx) * p.ny;
   const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= npix) return;
   const uint32_t Y = uint32_t(t / p.nx), X = uint32_t(t % p.nx);
-  // geometry, operation for operation in float with correct rounding
-  const float posx = __fadd_rn(p.start, __fmul_rn(float(X), p.dx));
-  const float posy = __fadd_rn(p.start, __fmul_rn(float(Y), p.dy));
-  const float ax = __fadd_rn(p.kx, posx), ay = __fadd_rn(p.ky, posy);
-  const float val = __fsub_rn(__fsub_rn(__fmul_rn(p.kmag, p.kmag), __fmul_rn(ax, ax)), __fmul_rn(ay, ay));
+  const EwaldGeom g{p.start, p.dx, p.dy, p.dz, p.kmag, p.kx, p.ky, p.kz, p.nx, p.ny, p.nz, p.interp, p.twod};
+  uint32_t Z0, Z1;
+  float w1;
+  int nplanes;
+  const bool isnan_px = !ewald_geometry(g, X, Y, Z0, Z1, w1, nplanes);
   const float nanv = __int_as_float(0x7fc00000);
-  bool isnan_px = (val < 0.f) || (X == p.nx - 1) || (Y == p.ny - 1);
-  uint32_t Z0 = 0, Z1 = 0;
-  float w1 = 0.f;  // weight of plane Z1
-  int nplanes = 1;
-  if (!isnan_px) {
-    const float posz = __fadd_rn(-p.kz, __fsqrt_rn(val));
-    if (p.interp == 0) {
-      if (!p.twod) {
-        const float r = roundf(__fdiv_rn(__fsub_rn(posz, p.start), p.dz));  // round(), uniaxial.h:749
-        Z0 = r <= 0.f ? 0u : uint32_t(r);
-      }
-      if (Z0 > p.nz - 1) isnan_px = true;
-    } else if (!p.twod) {
-      const float tz = __fdiv_rn(__fsub_rn(posz, p.start), p.dz);
-      Z0 = tz <= 0.f ? 0u : uint32_t(tz);
-      if (Z0 >= p.nz - 1) {
-        isnan_px = true;  // Z > Nz-1 is the reference's NaN rule; Z == Nz-1 would read outside the volume
-      } else {
-        Z1 = Z0 + 1;
-        nplanes = 2;
-        const float base = __fadd_rn(p.start, __fmul_rn(float(Z0), p.dz));
-        w1 = __fdiv_rn(__fsub_rn(posz, base), p.dz);
-      }
-    }
-  }
   float *img = p.images + t;
   if (isnan_px) {
     for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
@@ -1032,9 +1048,13 @@ __device__ __forceinline__ bool warp_sample(const float *__restrict__ src, int W
   return true;
 }
 
-__global__ void k_warp(const float *__restrict__ src, float *__restrict__ dst, int W, int H, WarpCoef c) {
+// blockIdx.y selects image src + y * src_stride -> dst + y * dst_stride.
+__global__ void k_warp(const float *__restrict__ src, float *__restrict__ dst, int W, int H, WarpCoef c,
+                       size_t src_stride = 0, size_t dst_stride = 0) {
   const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= size_t(W) * H) return;
+  src += blockIdx.y * src_stride;
+  dst += blockIdx.y * dst_stride;
   float v;
   if (warp_sample(src, W, H, c, int(t % W), int(t / W), v)) dst[t] = v;
 }
@@ -1042,12 +1062,12 @@ __global__ void k_warp(const float *__restrict__ src, float *__restrict__ dst, i
 // Rotates every per-angle image, masks and sums over angles in FP64, and
 // averages (src/cudaMain.cu:830-909, include/uniaxial.h:958-992).
 struct RotateParams {
-  const float *images;      // [nangles][P]
+  const float *images;      // [batch = blockIdx.y][nangles][P]
   const WarpCoef *coef;     // [nangles]
   int W, H;                 // NPP image: width = Ny, height = Nx
   uint32_t nangles;
   uint32_t rot_mask;
-  float *avg;               // [P]
+  float *avg;               // [batch][P]
 };
 
 __global__ void __launch_bounds__(256) k_rotate_average(RotateParams p) {
@@ -1055,11 +1075,12 @@ __global__ void __launch_bounds__(256) k_rotate_average(RotateParams p) {
   const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= npix) return;
   const int xd = int(t % p.W), yd = int(t / p.W);
+  const float *images = p.images + size_t(blockIdx.y) * p.nangles * npix;
   double sum = 0.0;
   uint32_t count = 0;
   for (uint32_t a = 0; a < p.nangles; ++a) {
     float v = __int_as_float(0x7fc00000);
-    warp_sample(p.images + size_t(a) * npix, p.W, p.H, p.coef[a], xd, yd, v);
+    warp_sample(images + size_t(a) * npix, p.W, p.H, p.coef[a], xd, yd, v);
     if (p.rot_mask) {
       if (isnan(v)) {
         v = 0.f;
@@ -1075,12 +1096,12 @@ __global__ void __launch_bounds__(256) k_rotate_average(RotateParams p) {
   } else {
     r = float(sum / double(p.nangles));
   }
-  p.avg[t] = r;
+  p.avg[size_t(blockIdx.y) * npix + t] = r;
 }
 
-__global__ void k_fill(float *dst, size_t n, float v) {
+__global__ void k_fill(float *dst, size_t n, float v, size_t stride = 0) {
   const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t < n) dst[t] = v;
+  if (t < n) dst[blockIdx.y * stride + t] = v;
 }
 
 }  // namespace cyr

@@ -67,7 +67,17 @@ typedef struct cyr_options {
   uint32_t max_streams;        /* MaxStreams (accepted; the engine schedules itself) */
   uint32_t rot_mask;           /* RotMask */
   uint32_t reference_frame;    /* 1 Lab, 0 Material (the reference's bool values) */
+  uint32_t strategy;           /* engine only (zero-initialised = auto): how the spectra are formed.
+                                  1 PER_ENERGY: tensor-entry spectra per energy (per angle in the
+                                  Material frame), as the reference's pipeline does;
+                                  2 FIELDS: the 7 M + 1 energy-independent morphology fields are
+                                  transformed once per request and combined per energy and angle
+                                  at the Ewald sample points (exact by linearity of the FFT);
+                                  0 AUTO: FIELDS when there are enough energies x angles to
+                                  amortise it and its volumes fit the device, else PER_ENERGY. */
 } cyr_options;
+
+enum { CYR_STRATEGY_AUTO = 0, CYR_STRATEGY_PER_ENERGY = 1, CYR_STRATEGY_FIELDS = 2 };
 
 /* Human-readable description of the last failure on this thread. */
 CYR_API const char *cyr_last_error(void);
@@ -116,7 +126,8 @@ CYR_API int cyr_required_device_bytes(const cyr_options *opt, size_t *bytes);
  * per energy (5 or 6 tensor entries, 3 for the MATERIAL frame), info[1] =
  * z planes kept after the z FFT (nz when not pruned), info[2] = first kept
  * shifted plane, info[3] = 1 when the z axis is pruned, info[4] = E angles,
- * info[5] = k vectors.
+ * info[5] = k vectors, info[6] = 1 when the FIELDS strategy is chosen,
+ * info[7] = packed field volumes, info[8] = energies per Ewald launch.
  */
 CYR_API int cyr_plan_info(const cyr_options *opt, uint32_t *info, uint32_t n);
 

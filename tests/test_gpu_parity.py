@@ -140,3 +140,42 @@ def test_long_z_axes_match_oracle(case):
     e = rel_err(got, want)
     assert e.max() <= TOL, e.max()
     assert nat.device_errors() == 0
+
+
+# FIELDS strategy: the morphology's energy independent fields are transformed once per request and
+# every energy and angle is combined from them (fields.cuh).  Same tolerance, same NaN masks.
+@pytest.mark.parametrize("name", PROJ)
+def test_field_strategy_matches_oracle_and_reference(name):
+    nat = native()
+    case = cases.CASES[name]
+    got = nat.cuda_main(options_for(case, strategy=2), cases.optical_constants(case), cases.voxels(case),
+                        streams_variant=case.algorithm == 1).astype(np.float64)
+    want = oracle.run_case(case)
+    r32 = np.fromfile(f"{GOLDEN}/ref_{name}_fp32.bin", np.float32).reshape(want.shape)
+    assert np.array_equal(np.isnan(got), np.isnan(want)), "NaN mask differs from the FP64 oracle"
+    assert np.array_equal(np.isnan(got), np.isnan(r32)), "NaN mask differs from the reference FP32 build"
+    e = rel_err(got, want)
+    assert e.max() <= TOL, e.max()
+
+
+@pytest.mark.parametrize("case", LONG_Z, ids=[c.name for c in LONG_Z])
+def test_field_strategy_long_z_axes(case):
+    nat = native()
+    got = nat.cuda_main(options_for(case, strategy=2), cases.optical_constants(case), cases.voxels(case),
+                        streams_variant=case.algorithm == 1).astype(np.float64)
+    want = oracle.run_case(case)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    e = rel_err(got, want)
+    assert e.max() <= TOL, e.max()
+
+
+def test_strategies_agree_and_auto_picks_fields_for_many_energies():
+    nat = native()
+    case = cases.Case("strat", 64, 64, 32, 3, [280.0, 283.0, 285.0, 288.0, 291.0, 296.0], seed=41,
+                      geometry="blobs", angles=(0.0, 170.0, 10.0))
+    per = nat.cuda_main(options_for(case, strategy=1), cases.optical_constants(case), cases.voxels(case))
+    fld = nat.cuda_main(options_for(case, strategy=2), cases.optical_constants(case), cases.voxels(case))
+    assert nat.plan_info(options_for(case))["fields"] == 1
+    assert np.array_equal(np.isnan(per), np.isnan(fld))
+    e = rel_err(fld.astype(np.float64), per.astype(np.float64))
+    assert e.max() <= TOL, e.max()
