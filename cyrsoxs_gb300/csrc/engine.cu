@@ -40,6 +40,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/cyrsoxs.h"
@@ -131,12 +132,13 @@ struct DeviceBuffer {
 // read back after the caller has synchronised (cyr_profile_end).
 enum Stage {
   kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kBuildZ,
-  kFieldMeans, kBuildFields, kEwaldFields, kNumStages
+  kFieldMeans, kBuildFields, kEwaldFields, kRotateGram, kFftRows, kFftColsY, kFftColsZ, kNumStages
 };
 const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_pass<y>", "k_fft_pass<z>", "k_dc",
                                              "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp",
                                              "k_moments", "k_entry_means", "k_build_fft_z",
-                                             "k_field_means", "k_build_fields", "k_ewald_fields"};
+                                             "k_field_means", "k_build_fields", "k_ewald_fields", "k_rotate_gram",
+                                             "k_fft_rows", "k_fft_cols<y>", "k_fft_cols<z>"};
 
 struct Profiler {
   bool active = false;
@@ -200,12 +202,22 @@ int get_context(DeviceContext **out) {
   return CYR_OK;
 }
 
+// Columns per block of the strided warp-FFT passes (one warp per column):
+// 8 along y (row stride), 16 along z (plane stride), the faster of the two on
+// GB300 for each.
+constexpr uint32_t kColsTxY = 8, kColsTxZ = 16;
+
 int setup_attrs(DeviceContext &ctx) {
   if (ctx.attrs_done) return CYR_OK;
   const int smem = int(kFftSmemBudget);
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+#define CYR_COLS_ATTR(V, T) \
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_COLS_ATTR(4, kColsTxY) CYR_COLS_ATTR(8, kColsTxY) CYR_COLS_ATTR(16, kColsTxY)
+  CYR_COLS_ATTR(4, kColsTxZ) CYR_COLS_ATTR(8, kColsTxZ) CYR_COLS_ATTR(16, kColsTxZ)
+#undef CYR_COLS_ATTR
   CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_CUDA(cudaFuncSetAttribute(k_build_fft_z<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -264,13 +276,12 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
   const size_t nvox = size_t(nx) * ny * nz;
   const float2 *tw = nullptr;
   CYR_TRY(get_twiddles(ctx, N, &tw));
-  const int slot = ctx.prof.begin(kFftX + axis, st);
+  const int slot = ctx.prof.begin(axis == 0 ? kFftRows : axis == 1 ? kFftColsY : kFftColsZ, st);
   if (axis == 0) {
     RowPassParams rp{data, uint32_t(size_t(ny) * nz * count), tw};
-    const size_t smem = (N + 8 * fpad_len(N)) * sizeof(float2);
+    const size_t smem = (N + 8 * N) * sizeof(float2);
     k_fft_rows<V><<<(rp.rows + 7) / 8, 256, smem, st>>>(rp);
   } else {
-    constexpr uint32_t TX = 8;
     ColPassParams cp{};
     cp.data = data;
     cp.nx = nx;
@@ -281,9 +292,16 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
       cp.others = ny, cp.ostride = nx, cp.estride = nx * ny;
     }
     cp.tw = tw;
-    const size_t smem = (N + TX * line_stride(N, TX)) * sizeof(float2);
-    const dim3 grid(((nx + TX - 1) / TX) * cp.others, count);
-    k_fft_cols<V><<<grid, TX * 32, smem, st>>>(cp);
+    auto launch = [&](auto txc) {
+      constexpr uint32_t TX = decltype(txc)::value;
+      const size_t smem = (N + TX * line_stride(N, TX)) * sizeof(float2);
+      const dim3 grid(((nx + TX - 1) / TX) * cp.others, count);
+      k_fft_cols<V, TX><<<grid, TX * 32, smem, st>>>(cp);
+    };
+    if (axis == 1)
+      launch(std::integral_constant<uint32_t, kColsTxY>{});
+    else
+      launch(std::integral_constant<uint32_t, kColsTxZ>{});
   }
   ctx.prof.end(slot, st);
   CYR_CUDA(cudaGetLastError());
@@ -368,11 +386,19 @@ struct Plan {
   uint32_t npk = 0;                     // packed field volumes
   uint32_t ebatch = 1;                  // energies per Ewald / rotation launch
   size_t off_fcoef = 0, off_kmag = 0, off_mat = 0;
+  uint32_t mom_zstep = 1;               // z planes between the moment samples (FIELDS)
 };
+
+// Bytes of one energy's Ewald output: Gram maps in the LAB frame (rotated by
+// k_rotate_gram), per-angle images in the MATERIAL frame (k_rotate_average).
+size_t image_bytes(const Plan &pl) {
+  if (pl.material_frame) return size_t(pl.nang) * pl.npix * sizeof(float);
+  return pl.npix * sizeof(float4) * (pl.nbasis == 3 ? 2 : 1);
+}
 
 // Device bytes of the FIELDS strategy: packed field spectra, per-batch images and averages.
 size_t field_bytes(const Plan &pl) {
-  return size_t(pl.npk) * pl.nvox * sizeof(float2) + size_t(pl.ebatch) * (pl.nang + 1) * pl.npix * sizeof(float) +
+  return size_t(pl.npk) * pl.nvox * sizeof(float2) + size_t(pl.ebatch) * (image_bytes(pl) + pl.npix * sizeof(float)) +
          pl.arena.size() + (num_fields(pl.nmat) + 2 * pl.npk) * sizeof(float2);
 }
 
@@ -638,10 +664,12 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
     pl.fields = o->strategy == CYR_STRATEGY_FIELDS;
   }
   {
-    const size_t img = size_t(pl.nang) * pl.npix * sizeof(float);
-    pl.ebatch = uint32_t(std::max<size_t>(1, std::min<size_t>(pl.ne, (size_t(96) << 20) / img)));
+    // per energy: Gram maps (LAB) or per-angle images (MATERIAL), kept within L2 for the rotation
+    const size_t img = image_bytes(pl);
+    pl.ebatch = uint32_t(std::max<size_t>(1, std::min<size_t>({size_t(pl.ne), size_t(32), (size_t(96) << 20) / img})));
   }
   if (pl.fields) {
+    pl.mom_zstep = std::max(1u, pl.nz / 16);  // 16 sampled planes
     // coef[e][v][j] = (alpha, beta): Nt_v(k) = sum_j alpha Z_j(k) + beta conj Z_j(-k), where
     // Z_j = F_2j + i F_2j+1 and field g = 7 m + f (f: u_x^2 u_y^2 u_z^2 u_xu_y u_xu_z u_yu_z phi_ui), T last
     const uint32_t nf = num_fields(pl.nmat), npk = pl.npk;
@@ -708,7 +736,7 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
 
 size_t request_bytes(const Plan &pl) {
   if (pl.fields) return field_bytes(pl) + pl.nmat * kMoments * sizeof(double) + 64 * sizeof(float2);
-  return pl.nvol * pl.vstride * sizeof(float2) + (pl.euler ? pl.nvox * pl.nmat * sizeof(float4) : 0) + size_t(pl.nang) * pl.npix * sizeof(float) + pl.npix * sizeof(float) +
+  return pl.nvol * pl.vstride * sizeof(float2) + (pl.euler ? pl.nvox * pl.nmat * sizeof(float4) : 0) + image_bytes(pl) + pl.npix * sizeof(float) +
          pl.arena.size() + 64 * sizeof(float2);
 }
 
@@ -753,11 +781,12 @@ int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const u
   CYR_TRY(ctx.fmean.ensure(nf * sizeof(float)));
   CYR_TRY(ctx.spec.ensure(size_t(npk) * pl.nvox * sizeof(float2)));
   CYR_TRY(ctx.dc.ensure(size_t(npk) * sizeof(float2)));
-  CYR_TRY(ctx.images.ensure(size_t(pl.ebatch) * pl.nang * pl.npix * sizeof(float)));
+  CYR_TRY(ctx.images.ensure(size_t(pl.ebatch) * image_bytes(pl)));
   CYR_TRY(ctx.avg.ensure(size_t(pl.ebatch) * pl.npix * sizeof(float)));
   float2 *spec = ctx.spec.as<float2>();
   int slot = ctx.prof.begin(kFieldMeans, st);
-  k_field_means<<<1, 128, 0, st>>>(ctx.moments.as<double>(), pl.nmat, pl.nvox, ctx.fmean.as<float>());
+  k_field_means<<<1, 128, 0, st>>>(ctx.moments.as<double>(), pl.nmat,
+                                   pl.npix * ((pl.nz + pl.mom_zstep - 1) / pl.mom_zstep), ctx.fmean.as<float>());
   ctx.prof.end(slot, st);
   CYR_CUDA(cudaGetLastError());
   FieldParams fp{};
@@ -807,10 +836,12 @@ int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const u
   fe.qz = reinterpret_cast<const float *>(dp + pl.off_qz);
   fe.nangles = pl.nang;
   fe.images = ctx.images.as<float>();
+  fe.gram = ctx.images.as<float4>();
   const size_t fsmem = size_t(6) * npk * sizeof(float4);
   const unsigned pix_blocks = unsigned((pl.npix + 255) / 256);
   const unsigned fpix_blocks = unsigned((pl.npix + kFieldEwaldThreads - 1) / kFieldEwaldThreads);
   const int W = int(pl.ny), H = int(pl.nx);  // the reference hands NPP width = Ny, height = Nx
+  const unsigned rot_tiles = unsigned(((W + kRotTile - 1) / kRotTile) * ((H + kRotTile - 1) / kRotTile));
   const WarpCoef *dwarp = reinterpret_cast<const WarpCoef *>(dp + pl.off_warp);
   const float *dmat = reinterpret_cast<const float *>(dp + pl.off_mat);
   const float fillv = o->rot_mask ? 0.f : std::numeric_limits<float>::quiet_NaN();
@@ -819,6 +850,7 @@ int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const u
     const KFrame &f = pl.frames[k];
     fe.kvx = f.k.x, fe.kvy = f.k.y, fe.kvz = f.k.z;
     fe.mat = dmat + size_t(k) * pl.nang * 18;
+    fe.ecoef = reinterpret_cast<const float *>(dp + pl.off_coef) + size_t(k) * pl.nang * pl.nbasis;
     RotateParams rp{};
     rp.images = ctx.images.as<float>();
     rp.coef = dwarp + size_t(k) * pl.nang;
@@ -826,14 +858,34 @@ int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const u
     rp.nangles = pl.nang;
     rp.rot_mask = o->rot_mask;
     rp.avg = ctx.avg.as<float>();
+    RotateGramParams rg{};
+    rg.gram = ctx.images.as<float4>();
+    rg.coef = rp.coef;
+    rg.ecoef = fe.ecoef;
+    rg.W = W, rg.H = H;
+    rg.nangles = pl.nang;
+    rg.rot_mask = o->rot_mask;
+    rg.avg = rp.avg;
     for (uint32_t e0 = 0; e0 < pl.ne; e0 += pl.ebatch) {
       const uint32_t nb = std::min(pl.ebatch, pl.ne - e0);
       fe.e0 = e0;
+      fe.nbatch = nb;
       slot = ctx.prof.begin(kEwaldFields, st);
-      k_ewald_fields<<<dim3(fpix_blocks, nb), kFieldEwaldThreads, fsmem, st>>>(fe);
+      const unsigned fgrid = fpix_blocks * nb;
+      if (pl.material_frame)
+        k_ewald_fields<0><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+      else if (pl.nbasis == 2)
+        k_ewald_fields<2><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+      else
+        k_ewald_fields<3><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
       ctx.prof.end(slot, st);
-      slot = ctx.prof.begin(kRotate, st);
-      k_rotate_average<<<dim3(pix_blocks, nb), 256, 0, st>>>(rp);
+      slot = ctx.prof.begin(pl.material_frame ? kRotate : kRotateGram, st);
+      if (pl.material_frame)
+        k_rotate_average<<<dim3(pix_blocks, nb), 256, 0, st>>>(rp);
+      else if (pl.nbasis == 2)
+        k_rotate_gram<2><<<dim3(rot_tiles, nb), kRotTile * kRotTile, 0, st>>>(rg);
+      else
+        k_rotate_gram<3><<<dim3(rot_tiles, nb), kRotTile * kRotTile, 0, st>>>(rg);
       ctx.prof.end(slot, st);
       float *dst = d_out + (size_t(e0) * pl.nk + k) * pl.npix;
       slot = ctx.prof.begin(kFill, st);
@@ -868,7 +920,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   CYR_CUDA(cudaMemsetAsync(ctx.errors.ptr, 0, sizeof(unsigned), st));
   if (!pl.fields) {
     CYR_TRY(ctx.spec.ensure(pl.nvol * pl.vstride * sizeof(float2)));
-    CYR_TRY(ctx.images.ensure(size_t(pl.nang) * pl.npix * sizeof(float)));
+    CYR_TRY(ctx.images.ensure(image_bytes(pl)));
     CYR_TRY(ctx.avg.ensure(pl.npix * sizeof(float)));
     CYR_TRY(ctx.dc.ensure(8 * sizeof(float2)));
   }
@@ -896,6 +948,8 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
     }
     mp.out = ctx.moments.as<double>();
     mp.conv = convert ? ctx.conv.as<float4>() : nullptr;
+    // the conversion needs every voxel; the means alone need only a subsample of planes
+    mp.zstep = convert ? 1u : pl.mom_zstep;
     mp.neg = ctx.flags.as<unsigned>();
     int nsm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx.device));
@@ -1056,6 +1110,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   };
   const unsigned pix_blocks = unsigned((pl.npix + 255) / 256);
   const int W = int(pl.ny), H = int(pl.nx);  // the reference hands NPP width = Ny, height = Nx
+  const unsigned rot_tiles = unsigned(((W + kRotTile - 1) / kRotTile) * ((H + kRotTile - 1) / kRotTile));
   const WarpCoef *dwarp = reinterpret_cast<const WarpCoef *>(dp + pl.off_warp);
   const float *dcoef = reinterpret_cast<const float *>(dp + pl.off_coef);
 
@@ -1080,8 +1135,12 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
         ep.nangles = pl.nang;
         ep.coef = dcoef + size_t(k) * pl.nang * pl.nbasis;
         ep.images = images;
+        ep.gram = reinterpret_cast<float4 *>(images);
         const int slot = ctx.prof.begin(kEwald, st);
-        k_ewald_angles<<<pix_blocks, 256, 0, st>>>(ep);
+        if (pl.nbasis == 2)
+          k_ewald_angles<2><<<pix_blocks, 256, 0, st>>>(ep);
+        else
+          k_ewald_angles<3><<<pix_blocks, 256, 0, st>>>(ep);
         ctx.prof.end(slot, st);
         CYR_CUDA(cudaGetLastError());
       } else {
@@ -1098,21 +1157,37 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
           ep.nangles = 1;
           ep.coef = dcoef + ka;  // nbasis == 1, coefficient 1
           ep.images = images + size_t(a) * pl.npix;
+          ep.gram = nullptr;
           const int slot = ctx.prof.begin(kEwald, st);
-          k_ewald_angles<<<pix_blocks, 256, 0, st>>>(ep);
+          k_ewald_angles<1><<<pix_blocks, 256, 0, st>>>(ep);
           ctx.prof.end(slot, st);
           CYR_CUDA(cudaGetLastError());
         }
       }
-      RotateParams rp{};
-      rp.images = images;
-      rp.coef = dwarp + size_t(k) * pl.nang;
-      rp.W = W, rp.H = H;
-      rp.nangles = pl.nang;
-      rp.rot_mask = o->rot_mask;
-      rp.avg = avg;
-      int slot = ctx.prof.begin(kRotate, st);
-      k_rotate_average<<<pix_blocks, 256, 0, st>>>(rp);
+      int slot = ctx.prof.begin(pl.material_frame ? kRotate : kRotateGram, st);
+      if (pl.material_frame) {
+        RotateParams rp{};
+        rp.images = images;
+        rp.coef = dwarp + size_t(k) * pl.nang;
+        rp.W = W, rp.H = H;
+        rp.nangles = pl.nang;
+        rp.rot_mask = o->rot_mask;
+        rp.avg = avg;
+        k_rotate_average<<<pix_blocks, 256, 0, st>>>(rp);
+      } else {
+        RotateGramParams rg{};
+        rg.gram = reinterpret_cast<const float4 *>(images);
+        rg.coef = dwarp + size_t(k) * pl.nang;
+        rg.ecoef = dcoef + size_t(k) * pl.nang * pl.nbasis;
+        rg.W = W, rg.H = H;
+        rg.nangles = pl.nang;
+        rg.rot_mask = o->rot_mask;
+        rg.avg = avg;
+        if (pl.nbasis == 2)
+          k_rotate_gram<2><<<rot_tiles, kRotTile * kRotTile, 0, st>>>(rg);
+        else
+          k_rotate_gram<3><<<rot_tiles, kRotTile * kRotTile, 0, st>>>(rg);
+      }
       ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());
       float *dst = d_out + (size_t(e) * pl.nk + k) * pl.npix;
@@ -1480,6 +1555,11 @@ extern "C" int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, u
     CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+#define CYR_COLS_ATTR(V, T) \
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_COLS_ATTR(4, kColsTxY) CYR_COLS_ATTR(8, kColsTxY) CYR_COLS_ATTR(16, kColsTxY)
+  CYR_COLS_ATTR(4, kColsTxZ) CYR_COLS_ATTR(8, kColsTxZ) CYR_COLS_ATTR(16, kColsTxZ)
+#undef CYR_COLS_ATTR
     stt.attrs = true;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);

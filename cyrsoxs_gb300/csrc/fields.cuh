@@ -32,8 +32,12 @@ constexpr int kFieldsPerMaterial = 7;
 __host__ __device__ constexpr uint32_t num_fields(uint32_t nmat) { return kFieldsPerMaterial * nmat + 1; }
 __host__ __device__ constexpr uint32_t num_packed(uint32_t nmat) { return (num_fields(nmat) + 1) / 2; }
 
-// Field means from the per-material volume moments (k_moments), T last.
-__global__ void k_field_means(const double *__restrict__ mom, uint32_t nmat, size_t nvox, float *__restrict__ out) {
+// Field means from the per-material moments (k_moments over nsamp voxels), T
+// last.  Any constant subtracted from a field changes only bin 0, which is
+// replaced, so the means need only be close (a z-plane subsample suffices);
+// they keep the FP32 rounding of the transform proportional to the
+// fluctuations.
+__global__ void k_field_means(const double *__restrict__ mom, uint32_t nmat, size_t nsamp, float *__restrict__ out) {
   const uint32_t nf = num_fields(nmat);
   for (uint32_t g = threadIdx.x; g < nf; g += blockDim.x) {
     double v = 0.0;
@@ -45,7 +49,7 @@ __global__ void k_field_means(const double *__restrict__ mom, uint32_t nmat, siz
         v += M[0] + M[1] + M[2] + M[6];
       }
     }
-    out[g] = float(v / double(nvox));
+    out[g] = float(v / double(nsamp));
   }
 }
 
@@ -118,20 +122,30 @@ struct FieldEwaldParams {
   EwaldGeom g;           // kmag, kx, ky, kz filled per energy
   const float *qx, *qy, *qz;
   uint32_t nangles;
-  const float *mat;      // [nangles][3][6]
-  float *images;         // [batch][nangles][npix]
+  const float *mat;      // NB = 0: [nangles][3][6]
+  const float *ecoef;    // NB > 0: [nangles][NB] E components of the LAB angle basis
+  float *images;         // NB = 0: [batch][nangles][npix]
+  float4 *gram;          // NB > 0: Gram maps [batch][npix][NQ]
+  uint32_t nbatch;       // energies of this launch
 };
 
 constexpr int kFieldEwaldThreads = 128;
+constexpr int kFieldGather = 4;  // packed volumes whose loads are issued together
 
+// NB = 2 or 3: LAB frame, Gram maps over the E basis (p(a) = sum_b E_b(a) Nt e_b),
+// rotated and averaged by k_rotate_gram.  NB = 0: any frame, p(a) = M(a) Nt per
+// angle, per-angle images.  The energy is the fastest block index, so the
+// blocks gathering one pixel tile for neighbouring energies (nearly the same
+// Ewald sphere) run together and share the gathered sectors in L2.
+template <int NB>
 __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldParams p) {
   extern __shared__ float4 fcoef[];  // [6][npk]
-  const uint32_t eb = blockIdx.y, e = p.e0 + eb;
+  const uint32_t eb = blockIdx.x % p.nbatch, e = p.e0 + eb;
   for (uint32_t t = threadIdx.x; t < 6 * p.npk; t += blockDim.x) fcoef[t] = p.coef[size_t(e) * 6 * p.npk + t];
   __syncthreads();
   const uint32_t nx = p.g.nx, ny = p.g.ny, nz = p.g.nz;
   const size_t npix = size_t(nx) * ny;
-  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const size_t t = size_t(blockIdx.x / p.nbatch) * blockDim.x + threadIdx.x;
   if (t >= npix) return;
   const uint32_t Y = uint32_t(t / nx), X = uint32_t(t % nx);
   EwaldGeom g = p.g;
@@ -141,14 +155,23 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   float w1;
   int nplanes;
   float *img = p.images + size_t(eb) * p.nangles * npix + t;
+  constexpr int NBG = NB > 0 ? NB : 1;
+  float4 *gm = p.gram + (size_t(eb) * npix + t) * GramLayout<NBG>::NQ;
   if (!ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes)) {
-    const float nanv = __int_as_float(0x7fc00000);
-    for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
+    if constexpr (NB > 0) {
+      gram_store_nan<NB>(gm);
+    } else {
+      const float nanv = __int_as_float(0x7fc00000);
+      for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
+    }
     return;
   }
   const uint32_t ux = igor(X, nx), uy = igor(Y, ny);
   const uint32_t mx = ux ? nx - ux : 0u, my = uy ? ny - uy : 0u;
-  float2 N[2][6];
+  const float d = g.kmag * g.kmag;
+  constexpr int NG = NB > 0 ? NB * (NB + 1) / 2 : 1;
+  float G[NG] = {};
+  float2 Nk[NB > 0 ? 1 : 2][6];  // NB = 0 keeps both planes' entries for the angle loop
   float Q[2][3];
   for (int pl = 0; pl < nplanes; ++pl) {
     const uint32_t uz = g.twod ? 0u : igor(zs[pl], nz);
@@ -156,47 +179,76 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
     const bool is_dc = ux == 0 && uy == 0 && uz == 0;
     const size_t i0 = size_t(ux) + size_t(uy) * nx + size_t(uz) * npix;
     const size_t i1 = size_t(mx) + size_t(my) * nx + size_t(mz) * npix;
+    float2 N[6];
 #pragma unroll
-    for (int v = 0; v < 6; ++v) N[pl][v] = make_float2(0.f, 0.f);
-    const float2 *zj = p.zspec;
-#pragma unroll 2
-    for (uint32_t j = 0; j < p.npk; ++j, zj += p.nvox) {
-      float2 a, b;
-      if (is_dc) {
-        a = b = p.zdc[j];
-      } else {
-        a = __ldg(&zj[i0]);
-        b = __ldg(&zj[i1]);
+    for (int v = 0; v < 6; ++v) N[v] = make_float2(0.f, 0.f);
+    for (uint32_t j0 = 0; j0 < p.npk; j0 += kFieldGather) {
+      float2 za[kFieldGather], zb[kFieldGather];
+#pragma unroll
+      for (int q = 0; q < kFieldGather; ++q) {
+        const uint32_t j = j0 + q;
+        za[q] = zb[q] = make_float2(0.f, 0.f);
+        if (j < p.npk) {
+          if (is_dc) {
+            za[q] = zb[q] = p.zdc[j];
+          } else {
+            const float2 *zj = p.zspec + size_t(j) * p.nvox;
+            za[q] = __ldg(&zj[i0]);
+            zb[q] = __ldg(&zj[i1]);
+          }
+        }
       }
-      b.y = -b.y;  // conj Z_j(-k)
 #pragma unroll
-      for (int v = 0; v < 6; ++v) {
-        const float4 c = fcoef[v * p.npk + j];
-        N[pl][v].x += c.x * a.x - c.y * a.y + c.z * b.x - c.w * b.y;
-        N[pl][v].y += c.x * a.y + c.y * a.x + c.z * b.y + c.w * b.x;
+      for (int q = 0; q < kFieldGather; ++q) {
+        const uint32_t j = j0 + q;
+        if (j >= p.npk) break;
+        const float2 a = za[q], b = make_float2(zb[q].x, -zb[q].y);  // b = conj Z_j(-k)
+#pragma unroll
+        for (int v = 0; v < 6; ++v) {
+          const float4 c = fcoef[v * p.npk + j];
+          N[v].x += c.x * a.x - c.y * a.y + c.z * b.x - c.w * b.y;
+          N[v].y += c.x * a.y + c.y * a.x + c.z * b.y + c.w * b.x;
+        }
       }
     }
     Q[pl][0] = g.kx + p.qx[X];
     Q[pl][1] = g.ky + p.qy[Y];
     Q[pl][2] = g.kz + (g.twod ? 0.f : p.qz[zs[pl]]);
-  }
-  const float d = g.kmag * g.kmag;
-  const float w0 = 1.f - w1;
-  for (uint32_t a = 0; a < p.nangles; ++a) {
-    const float *M = p.mat + size_t(a) * 18;
-    float I[2];
-    for (int pl = 0; pl < nplanes; ++pl) {
-      float2 pc[3];
+    if constexpr (NB > 0) {
+      // symmetric entry (c, b) of Nt: volumes xx xy xz yy yz zz
+      float2 P[3][NB];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int v = 0; v < 6; ++v) acc = cfma(__ldg(&M[c * 6 + v]), N[pl][v], acc);
-        pc[c] = acc;
+      for (int b = 0; b < NB; ++b) {
+        P[0][b] = N[b == 0 ? 0 : b == 1 ? 1 : 2];
+        P[1][b] = N[b == 0 ? 1 : b == 1 ? 3 : 4];
+        P[2][b] = N[b == 0 ? 2 : b == 1 ? 4 : 5];
       }
-      I[pl] = intensity(Q[pl][0], Q[pl][1], Q[pl][2], d, pc[0], pc[1], pc[2]);
+      gram_add<NB>(Q[pl], d, P, nplanes == 2 ? (pl == 0 ? 1.f - w1 : w1) : 1.f, G);
+    } else {
+#pragma unroll
+      for (int v = 0; v < 6; ++v) Nk[pl][v] = N[v];
     }
-    img[size_t(a) * npix] = nplanes == 2 ? w0 * I[0] + w1 * I[1] : I[0];
+  }
+  if constexpr (NB > 0) {
+    gram_store<NB>(gm, G);
+  } else {
+    const float w0 = 1.f - w1;
+    for (uint32_t a = 0; a < p.nangles; ++a) {
+      const float *M = p.mat + size_t(a) * 18;
+      float I[2];
+      for (int pl = 0; pl < nplanes; ++pl) {
+        float2 pc[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int v = 0; v < 6; ++v) acc = cfma(__ldg(&M[c * 6 + v]), Nk[pl][v], acc);
+          pc[c] = acc;
+        }
+        I[pl] = intensity(Q[pl][0], Q[pl][1], Q[pl][2], d, pc[0], pc[1], pc[2]);
+      }
+      img[size_t(a) * npix] = nplanes == 2 ? w0 * I[0] + w1 * I[1] : I[0];
+    }
   }
 }
 

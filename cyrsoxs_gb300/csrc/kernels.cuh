@@ -147,6 +147,7 @@ struct MomentParams {
   double *out;      // [nmat][kMoments], accumulated
   float4 *conv;     // Euler only: (sqrt(phi_a) s, phi_ui) per material and voxel, or null
   unsigned *neg;    // set when some phi_a < 0
+  uint32_t zstep;   // sample every zstep-th z plane (1: all; must be 1 with conv)
 };
 
 template <int MORPH>
@@ -159,7 +160,9 @@ __global__ void __launch_bounds__(256) k_moments(MomentParams p) {
 #pragma unroll
   for (int q = 0; q < kMoments; ++q) acc[q] = 0.f;
   const size_t stride = size_t(gridDim.x) * blockDim.x;
-  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
+  const size_t plane = size_t(p.nx) * p.ny, nsamp = plane * ((p.nz + p.zstep - 1) / p.zstep);
+  for (size_t s = size_t(blockIdx.x) * blockDim.x + threadIdx.x; s < nsamp; s += stride) {
+    const size_t i = p.zstep == 1 ? s : (s / plane) * p.zstep * plane + s % plane;
     float sx, sy, sz, pa, pui;
     director<MORPH>(__ldg(&p.vox[m * p.nvox + i]), sx, sy, sz, pa, pui);
     if (MORPH == 0 && p.conv) {
@@ -546,18 +549,28 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
 // One warp owns one line.  Lane t holds x[t + 32 i] in v[i] (natural order)
 // on entry and X[t + 32 i] on exit.  Each Stockham stage of radix R <= V runs
 // V / R butterflies per lane on registers; between stages the lanes exchange
-// through the warp's own line in shared memory (padded p -> p + p / 8, which
-// keeps the stride-R and stride-1 patterns free of bank conflicts), so only
-// __syncwarp is needed.  The last stage's outputs land in natural order in
-// registers.  Twiddles W_N^m come from a shared table generated in FP64.
+// through the warp's own line in shared memory (swizzled, swz: free of bank
+// conflicts for every access of the plan), so only __syncwarp is needed.  The last stage's outputs land in natural order in
+// registers.  Twiddles W_N^m (generated in FP64) are staged per stage in the
+// order the lanes read them (warp_twiddles).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t fpad(uint32_t p) { return p + (p >> 3); }
-__host__ __device__ constexpr uint32_t fpad_len(uint32_t n) { return n + (n >> 3) + 1; }
-// Stride between the padded lines of TX interleaved columns: congruent to
-// 16 / TX modulo 16, so a half-warp touching TX columns x (16 / TX)
-// consecutive positions hits 16 distinct 8-byte bank pairs.
+// Shared-memory slot of element p of a line: the 8-byte bank (the low 4 bits)
+// is XORed with a GF(2)-linear function of the higher bits.  The masks were
+// found by an exhaustive check of every access of the V = 4, 8, 16 plans
+// (contiguous reads, each stage's strided stores) and of the TX-column tile
+// copies (TX = 2..16, line_stride below): no half-warp access puts two lanes
+// on one bank.  A bijection on [0, N), so lines need no padding.
+__device__ __forceinline__ uint32_t swz(uint32_t p) {
+  const uint32_t h = p >> 4;
+  const uint32_t x = ((h & 1u) ? 10u : 0u) ^ ((h & 2u) ? 15u : 0u) ^ ((h & 4u) ? 12u : 0u) ^
+                     ((h & 8u) ? 3u : 0u) ^ ((h & 16u) ? 12u : 0u);
+  return p ^ x;
+}
+// Stride between the lines of TX interleaved columns: congruent to 16 / TX
+// (1 for TX >= 16) modulo 16, so a half-warp touching TX columns x (16 / TX)
+// consecutive positions hits 16 distinct 8-byte banks.
 __host__ __device__ constexpr uint32_t line_stride(uint32_t n, uint32_t tx) {
-  return ((fpad_len(n) + 15u) & ~15u) + (tx >= 16 ? 0u : 16u / tx);
+  return ((n + 15u) & ~15u) + (tx >= 16 ? 1u : 16u / tx);
 }
 
 template <int V>
@@ -573,12 +586,35 @@ struct WarpPlan {
   __host__ __device__ static constexpr int radix(int s) { return s < NFULL ? MAXR : (REM == 2 ? 4 : 2); }
 };
 
+// Shared twiddle tables of the warp FFT: stage s > 0 (NS > 1, radix R) holds
+// W_N^(k r N / (NS R)) at [NS - R0 + k (R - 1) + r - 1] for k < NS, 1 <= r < R
+// (N - R0 entries in all).  The lanes of a half-warp read 16 consecutive k,
+// addresses an odd R - 1 apart: 16 distinct banks, where the strided table
+// W_N^(k r TWS) put up to 8 lanes on one bank.
+template <int V>
+__device__ __forceinline__ void warp_twiddles(float2 *dst, const float2 *__restrict__ tw_n) {
+  using P = WarpPlan<V>;
+  constexpr uint32_t N = P::N, R0 = P::radix(0);
+  for (uint32_t t = threadIdx.x; t < N - R0; t += blockDim.x) {
+    uint32_t ns = R0, base = 0;
+#pragma unroll
+    for (int s = 1; s < P::NSTAGES; ++s) {
+      const uint32_t R = P::radix(s), cnt = ns * (R - 1);
+      if (t >= base && t < base + cnt) {
+        const uint32_t u = t - base, k = u / (R - 1), r = u % (R - 1) + 1;
+        dst[t] = __ldg(&tw_n[k * r * (N / (ns * R))]);
+      }
+      base += cnt;
+      ns *= R;
+    }
+  }
+}
+
 template <int V, int R, int NS, bool LAST>
 __device__ __forceinline__ void warp_stage(float2 (&v)[V], float2 *line, const float2 *__restrict__ tw,
                                            uint32_t lane) {
-  constexpr int N = 32 * V;
-  constexpr int B = V / R;          // butterflies per lane
-  constexpr int TWS = N / (NS * R); // twiddle stride
+  constexpr int B = V / R;                          // butterflies per lane
+  constexpr int TWOFF = NS > 1 ? NS - WarpPlan<V>::radix(0) : 0;  // this stage's table (warp_twiddles)
 #pragma unroll
   for (int q = 0; q < B; ++q) {
     const uint32_t j = lane + 32 * q;
@@ -588,7 +624,7 @@ __device__ __forceinline__ void warp_stage(float2 (&v)[V], float2 *line, const f
     for (int r = 0; r < R; ++r) w[r] = v[q + r * B];
     if (NS > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) w[r] = cmul(w[r], tw[k * r * TWS]);
+      for (int r = 1; r < R; ++r) w[r] = cmul(w[r], tw[TWOFF + k * (R - 1) + r - 1]);
     }
     if (R == 2) dft2(w);
     if (R == 4) dft4(w[0], w[1], w[2], w[3]);
@@ -599,13 +635,13 @@ __device__ __forceinline__ void warp_stage(float2 (&v)[V], float2 *line, const f
     } else {
       const uint32_t base = (j / NS) * NS * R + k;
 #pragma unroll
-      for (int r = 0; r < R; ++r) line[fpad(base + r * NS)] = w[r];
+      for (int r = 0; r < R; ++r) line[swz(base + r * NS)] = w[r];
     }
   }
   if (!LAST) {
     __syncwarp();
 #pragma unroll
-    for (int i = 0; i < V; ++i) v[i] = line[fpad(lane + 32 * i)];
+    for (int i = 0; i < V; ++i) v[i] = line[swz(lane + 32 * i)];
     __syncwarp();
   }
 }
@@ -638,8 +674,8 @@ __global__ void __launch_bounds__(256) k_fft_rows(RowPassParams p) {
   extern __shared__ float2 smem[];
   float2 *tws = smem;                              // N
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float2 *line = smem + N + warp * fpad_len(N);
-  for (uint32_t t = threadIdx.x; t < N; t += blockDim.x) tws[t] = __ldg(&p.tw[t]);
+  float2 *line = smem + N + warp * N;
+  warp_twiddles<V>(tws, p.tw);
   __syncthreads();
   const uint32_t row = blockIdx.x * (blockDim.x >> 5) + warp;
   if (row >= p.rows) return;
@@ -666,43 +702,43 @@ struct ColPassParams {
   const float2 *tw;
 };
 
-template <int V>
-__global__ void __launch_bounds__(256) k_fft_cols(ColPassParams p) {
-  constexpr uint32_t N = 32 * V, TX = 8, L = line_stride(N, TX);
+template <int V, int TX>
+__global__ void __launch_bounds__(TX * 32) k_fft_cols(ColPassParams p) {
+  constexpr uint32_t N = 32 * V, L = line_stride(N, TX), NT = TX * 32;
   extern __shared__ float2 smem[];
   float2 *tws = smem, *tile = smem + N;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t nxt = (p.nx + TX - 1) / TX;
   const uint32_t xt = blockIdx.x % nxt, other = blockIdx.x / nxt, x0 = xt * TX;
-  const uint32_t valid = min(TX, p.nx - x0);
+  const uint32_t valid = min(uint32_t(TX), p.nx - x0);
   float2 *g = p.data + size_t(blockIdx.y) * p.vstride + size_t(other) * p.ostride + x0;
   const uint32_t l = threadIdx.x % TX, i0 = threadIdx.x / TX;  // compile-time TX: shifts
-  constexpr uint32_t ISTEP = 256 / TX;
+  constexpr uint32_t ISTEP = NT / TX;
   if (l < valid) {
 #pragma unroll 4
-    for (uint32_t i = i0; i < N; i += ISTEP) cp_async8(&tile[l * L + fpad(i)], &g[l + i * p.estride]);
+    for (uint32_t i = i0; i < N; i += ISTEP) cp_async8(&tile[l * L + swz(i)], &g[l + i * p.estride]);
   } else {
-    for (uint32_t i = i0; i < N; i += ISTEP) tile[l * L + fpad(i)] = make_float2(0.f, 0.f);
+    for (uint32_t i = i0; i < N; i += ISTEP) tile[l * L + swz(i)] = make_float2(0.f, 0.f);
   }
-  for (uint32_t t = threadIdx.x; t < N; t += blockDim.x) tws[t] = __ldg(&p.tw[t]);
+  warp_twiddles<V>(tws, p.tw);
   cp_async_wait_all();
   __syncthreads();
-  float2 *line = tile + warp * L;
+  float2 *line = tile + warp * L;  // one warp per column
   float2 v[V];
 #pragma unroll
-  for (int i = 0; i < V; ++i) v[i] = line[fpad(lane + 32 * i)];
+  for (int i = 0; i < V; ++i) v[i] = line[swz(lane + 32 * i)];
   __syncwarp();
   warp_fft<V>(v, line, tws, lane);
 #pragma unroll
-  for (int i = 0; i < V; ++i) line[fpad(lane + 32 * i)] = v[i];
+  for (int i = 0; i < V; ++i) line[swz(lane + 32 * i)] = v[i];
   __syncthreads();
   if (l < valid) {
 #pragma unroll 4
-    for (uint32_t i = i0; i < N; i += ISTEP) g[l + i * p.estride] = tile[l * L + fpad(i)];
+    for (uint32_t i = i0; i < N; i += ISTEP) g[l + i * p.estride] = tile[l * L + swz(i)];
   }
 }
 
-// Tensor build fused with the z-axis FFT, keeping only the z planes the Ewald
+// Warp-FFT form of k_build_fft_z// Tensor build fused with the z-axis FFT, keeping only the z planes the Ewald
 // projection can read.  A block owns TX consecutive x columns at one y, over
 // all z: it computes the nvol entry volumes for those columns into shared
 // memory, transforms them along z, and writes planes [zlo, zlo + kz) of the
@@ -776,7 +812,7 @@ __global__ void __launch_bounds__(256) k_build_fft_z_warp(BuildZParams p, const 
   float2 *tws = smem, *lines = smem + NZ;
   const uint32_t nxt = (b.nx + TX - 1) / TX;
   const uint32_t xt = blockIdx.x % nxt, y = blockIdx.x / nxt, x0 = xt * TX;
-  for (uint32_t t = threadIdx.x; t < NZ; t += blockDim.x) tws[t] = __ldg(&p.az.tw[t]);
+  warp_twiddles<V>(tws, p.az.tw);
   // With p.stage the block's morphology tile [m][z][TX] is copied into shared
   // memory with 16-byte cp.async first, so all of its loads are in flight at once.
   const uint32_t nl = nvol * TX * L;
@@ -814,7 +850,7 @@ __global__ void __launch_bounds__(256) k_build_fft_z_warp(BuildZParams p, const 
     }
 #pragma unroll
     for (int c = 0; c < 6; ++c)
-      if (uint32_t(c) < nvol) lines[(c * TX + l) * L + fpad(z)] = v[c];
+      if (uint32_t(c) < nvol) lines[(c * TX + l) * L + swz(z)] = v[c];
   }
   __syncthreads();
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
@@ -822,11 +858,11 @@ __global__ void __launch_bounds__(256) k_build_fft_z_warp(BuildZParams p, const 
     float2 *line = lines + li * L;
     float2 v[V];
 #pragma unroll
-    for (int i = 0; i < V; ++i) v[i] = line[fpad(lane + 32 * i)];
+    for (int i = 0; i < V; ++i) v[i] = line[swz(lane + 32 * i)];
     __syncwarp();
     warp_fft<V>(v, line, tws, lane);
 #pragma unroll
-    for (int i = 0; i < V; ++i) line[fpad(lane + 32 * i)] = v[i];
+    for (int i = 0; i < V; ++i) line[swz(lane + 32 * i)] = v[i];
     __syncwarp();
   }
   __syncthreads();
@@ -835,7 +871,7 @@ __global__ void __launch_bounds__(256) k_build_fft_z_warp(BuildZParams p, const 
   for (uint32_t c = 0; c < nvol; ++c) {
     const float2 *ln = lines + (c * TX + l) * L;
     float2 *oc = out + size_t(c) * p.kz * plane;
-    for (uint32_t q = z0; q < p.kz; q += ZSTEP) oc[q * plane] = ln[fpad(igor(p.zlo + q, NZ))];
+    for (uint32_t q = z0; q < p.kz; q += ZSTEP) oc[q * plane] = ln[swz(igor(p.zlo + q, NZ))];
   }
 }
 
@@ -889,6 +925,7 @@ struct EwaldParams {
   uint32_t zlo, nplanes;
   unsigned int *errors;   // incremented when a needed plane is not stored
   uint32_t nbasis;        // 1..3
+  float4 *gram;           // when set: Gram maps [P][NQ] instead of per-angle images
   uint32_t vol[3][3];     // vol[c][b]: volume holding component c of basis b
   uint32_t nangles;
   const float *coef;      // [nangles][nbasis]
@@ -905,6 +942,76 @@ struct EwaldParams {
 __device__ __forceinline__ uint32_t igor(uint32_t j, uint32_t n) {
   const uint32_t h = n / 2;
   return j <= h ? h - j : n + h - j;
+}
+
+// Scattered field of one polarization basis vector: t = d p - Q (Q . p).
+__device__ __forceinline__ void scatter_t(const float Q[3], float d, float2 p0, float2 p1, float2 p2, float2 t[3]) {
+  const float2 qp = make_float2(Q[0] * p0.x + Q[1] * p1.x + Q[2] * p2.x, Q[0] * p0.y + Q[1] * p1.y + Q[2] * p2.y);
+  t[0] = make_float2(d * p0.x - Q[0] * qp.x, d * p0.y - Q[0] * qp.y);
+  t[1] = make_float2(d * p1.x - Q[1] * qp.x, d * p1.y - Q[1] * qp.y);
+  t[2] = make_float2(d * p2.x - Q[2] * qp.x, d * p2.y - Q[2] * qp.y);
+}
+
+// Re(a . conj b) of two complex 3-vectors.
+__device__ __forceinline__ float redot3(const float2 a[3], const float2 b[3]) {
+  return a[0].x * b[0].x + a[0].y * b[0].y + a[1].x * b[1].x + a[1].y * b[1].y + a[2].x * b[2].x + a[2].y * b[2].y;
+}
+
+// Gram form of the angle loop.  The polarization of E angle a is
+// p(a) = sum_b E_b(a) P_b over NB basis vectors P_b, and t is linear in p, so
+//   I(a) = |sum_b E_b t_b|^2 = sum_{b,b'} E_b E_b' G_bb',  G_bb' = Re(t_b . conj t_b'),
+// and the plane interpolation (linear in I) applies to G.  G is accumulated
+// once per pixel; each angle then costs NB (NB + 1) / 2 multiply-adds.
+template <int NB>
+__device__ __forceinline__ void gram_add(const float Q[3], float d, const float2 (&P)[3][NB], float w,
+                                         float (&G)[NB * (NB + 1) / 2]) {
+  float2 t[NB][3];
+#pragma unroll
+  for (int b = 0; b < NB; ++b) scatter_t(Q, d, P[0][b], P[1][b], P[2][b], t[b]);
+  int q = 0;
+#pragma unroll
+  for (int b = 0; b < NB; ++b)
+#pragma unroll
+    for (int b2 = b; b2 < NB; ++b2) G[q++] += w * redot3(t[b], t[b2]);
+}
+
+template <int NB>
+__device__ __forceinline__ float gram_intensity(const float (&G)[NB * (NB + 1) / 2], const float *__restrict__ cf) {
+  float e[NB];
+#pragma unroll
+  for (int b = 0; b < NB; ++b) e[b] = __ldg(&cf[b]);
+  float I = 0.f;
+  int q = 0;
+#pragma unroll
+  for (int b = 0; b < NB; ++b)
+#pragma unroll
+    for (int b2 = b; b2 < NB; ++b2) I += (b == b2 ? 1.f : 2.f) * e[b] * e[b2] * G[q++];
+  return I;
+}
+
+// Gram maps: NB = 1 or 2 -> one float4 per pixel (G00 [G01 G11]), NB = 3 -> two
+// (G00 G01 G02 G11 | G12 G22); a NaN pixel stores NaN in every component.
+template <int NB>
+struct GramLayout {
+  static constexpr int NG = NB * (NB + 1) / 2;
+  static constexpr int NQ = (NG + 3) / 4;
+};
+
+template <int NB>
+__device__ __forceinline__ void gram_store(float4 *gm, const float (&G)[NB * (NB + 1) / 2]) {
+  constexpr int NG = GramLayout<NB>::NG, NQ = GramLayout<NB>::NQ;
+  float v[4 * NQ];
+#pragma unroll
+  for (int q = 0; q < 4 * NQ; ++q) v[q] = q < NG ? G[q] : 0.f;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) gm[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+
+template <int NB>
+__device__ __forceinline__ void gram_store_nan(float4 *gm) {
+  const float n = __int_as_float(0x7fc00000);
+#pragma unroll
+  for (int q = 0; q < GramLayout<NB>::NQ; ++q) gm[q] = make_float4(n, n, n, n);
 }
 
 __device__ __forceinline__ float intensity(float Q0, float Q1, float Q2, float d, float2 p0, float2 p1, float2 p2) {
@@ -957,27 +1064,32 @@ __device__ __forceinline__ bool ewald_geometry(const EwaldGeom &g, uint32_t X, u
   return true;
 }
 
+template <int NB>
 __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
   const size_t npix = size_t(p.nx) * p.ny;
   const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= npix) return;
   const uint32_t Y = uint32_t(t / p.nx), X = uint32_t(t % p.nx);
   const EwaldGeom g{p.start, p.dx, p.dy, p.dz, p.kmag, p.kx, p.ky, p.kz, p.nx, p.ny, p.nz, p.interp, p.twod};
-  uint32_t Z0, Z1;
+  uint32_t zs[2];
   float w1;
   int nplanes;
-  const bool isnan_px = !ewald_geometry(g, X, Y, Z0, Z1, w1, nplanes);
+  const bool isnan_px = !ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes);
   const float nanv = __int_as_float(0x7fc00000);
   float *img = p.images + t;
+  float4 *gm = p.gram ? p.gram + t * GramLayout<NB>::NQ : nullptr;
   if (isnan_px) {
+    if (gm) {
+      gram_store_nan<NB>(gm);
+      return;
+    }
     for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
     return;
   }
-  // gather the basis spectra at the (one or two) planes
+  // gather the basis spectra at the (one or two) planes and accumulate their Gram matrix
   const uint32_t ux = igor(X, p.nx), uy = igor(Y, p.ny);
-  float2 P[2][3][3];  // [plane][component][basis]
-  float Q[2][3];
-  const uint32_t zs[2] = {Z0, Z1};
+  const float d = p.kmag * p.kmag;
+  float G[NB * (NB + 1) / 2] = {};
   for (int pl = 0; pl < nplanes; ++pl) {
     const uint32_t uz = p.twod ? 0u : igor(zs[pl], p.nz);
     uint32_t pz = uz;
@@ -985,39 +1097,32 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
       pz = zs[pl] - p.zlo;
       if (zs[pl] < p.zlo || pz >= p.nplanes) {  // the host's plane range missed this pixel
         atomicAdd(p.errors, 1u);
+        if (gm) {
+          gram_store_nan<NB>(gm);
+          return;
+        }
         for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
         return;
       }
     }
     const bool is_dc = ux == 0 && uy == 0 && uz == 0;
     const size_t idx = size_t(ux) + size_t(uy) * p.nx + size_t(pz) * p.nx * p.ny;
-    for (uint32_t b = 0; b < p.nbasis; ++b)
+    float2 P[3][NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const uint32_t v = p.vol[c][b];
-        P[pl][c][b] = is_dc ? p.dc[v] : __ldg(&p.spec[size_t(v) * p.nvox + idx]);
+        P[c][b] = is_dc ? p.dc[v] : __ldg(&p.spec[size_t(v) * p.nvox + idx]);
       }
-    Q[pl][0] = p.kx + p.qx[X];
-    Q[pl][1] = p.ky + p.qy[Y];
-    Q[pl][2] = p.kz + (p.twod ? 0.f : p.qz[zs[pl]]);
+    const float Q[3] = {p.kx + p.qx[X], p.ky + p.qy[Y], p.kz + (p.twod ? 0.f : p.qz[zs[pl]])};
+    gram_add<NB>(Q, d, P, nplanes == 2 ? (pl == 0 ? 1.f - w1 : w1) : 1.f, G);
   }
-  const float d = p.kmag * p.kmag;
-  const float w0 = 1.f - w1;
-  for (uint32_t a = 0; a < p.nangles; ++a) {
-    const float *cf = p.coef + size_t(a) * p.nbasis;
-    float I[2];
-    for (int pl = 0; pl < nplanes; ++pl) {
-      float2 pc[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float2 acc = make_float2(0.f, 0.f);
-        for (uint32_t b = 0; b < p.nbasis; ++b) acc = cfma(cf[b], P[pl][c][b], acc);
-        pc[c] = acc;
-      }
-      I[pl] = intensity(Q[pl][0], Q[pl][1], Q[pl][2], d, pc[0], pc[1], pc[2]);
-    }
-    img[size_t(a) * npix] = nplanes == 2 ? w0 * I[0] + w1 * I[1] : I[0];
+  if (gm) {
+    gram_store<NB>(gm, G);
+    return;
   }
+  for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = gram_intensity<NB>(G, p.coef + size_t(a) * NB);
 }
 
 // ---------------------------------------------------------------------------
@@ -1029,6 +1134,33 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
 struct WarpCoef {
   float a00, a01, a02, a10, a11, a12;
 };
+
+// Source corners and fractions of destination pixel (xd, yd); false when the
+// source point lies outside the image (the destination keeps its value).
+struct WarpTap {
+  int i00, i01, i10, i11;  // y0 x0, y0 x1, y1 x0, y1 x1 (row-major, width W)
+  float fx, fy;
+};
+
+__device__ __forceinline__ bool warp_tap(int W, int H, const WarpCoef &c, int xd, int yd, WarpTap &tp) {
+  const float fx_ = float(xd), fy_ = float(yd);
+  const float xs = __fadd_rn(__fmaf_rn(c.a00, fx_, __fmul_rn(c.a01, fy_)), c.a02);
+  const float ys = __fadd_rn(__fmaf_rn(c.a10, fx_, __fmul_rn(c.a11, fy_)), c.a12);
+  if (!(xs >= 0.f && xs <= float(W - 1) && ys >= 0.f && ys <= float(H - 1))) return false;
+  const int x0 = min(int(floorf(xs)), W - 1), y0 = min(int(floorf(ys)), H - 1);
+  const int x1 = min(x0 + 1, W - 1), y1 = min(y0 + 1, H - 1);
+  tp.i00 = y0 * W + x0, tp.i01 = y0 * W + x1, tp.i10 = y1 * W + x0, tp.i11 = y1 * W + x1;
+  tp.fx = __fsub_rn(xs, float(x0)), tp.fy = __fsub_rn(ys, float(y0));
+  return true;
+}
+
+// NPP's bilinear blend of the four corners A (y0 x0), B (y0 x1), C (y1 x0), D (y1 x1).
+__device__ __forceinline__ float warp_blend(float fx, float fy, float A, float B, float C, float D) {
+  const float gx = __fsub_rn(1.f, fx), gy = __fsub_rn(1.f, fy);
+  const float t0 = __fmaf_rn(gx, A, __fmul_rn(fx, B));
+  const float t1 = __fmaf_rn(gx, C, __fmul_rn(fx, D));
+  return __fmaf_rn(gy, t0, __fmul_rn(fy, t1));
+}
 
 __device__ __forceinline__ bool warp_sample(const float *__restrict__ src, int W, int H, const WarpCoef &c, int xd,
                                             int yd, float &out) {
@@ -1089,6 +1221,90 @@ __global__ void __launch_bounds__(256) k_rotate_average(RotateParams p) {
       }
     }
     sum += double(v);
+  }
+  float r;
+  if (p.rot_mask) {
+    r = count == 0 ? 0.f : float(sum / double(count));
+  } else {
+    r = float(sum / double(p.nangles));
+  }
+  p.avg[size_t(blockIdx.y) * npix + t] = r;
+}
+
+// Rotation and angle average from Gram maps (LAB frame): per angle a the
+// corners' Gram matrices are blended as NPP blends intensities, then
+// I(a) = sum_{b,b'} E_b(a) E_b'(a) G_bb' (the blend is linear, so this equals
+// blending the per-angle intensities).  Accumulation in FP64 as in
+// k_rotate_average.  The loads of kRotUnroll angles are issued together
+// (out-of-image angles read pixel 0 and are discarded).
+struct RotateGramParams {
+  const float4 *gram;       // [batch = blockIdx.y][P][NQ]
+  const WarpCoef *coef;     // [nangles]
+  const float *ecoef;       // [nangles][NB]
+  int W, H;
+  uint32_t nangles;
+  uint32_t rot_mask;
+  float *avg;               // [batch][P]
+};
+
+constexpr int kRotUnroll = 4;
+
+// Blocks own 16 x 16 destination tiles (a warp: 16 x 2), so the rotated
+// source taps of a warp stay within a few cache lines.
+constexpr int kRotTile = 16;
+
+template <int NB>
+__global__ void __launch_bounds__(kRotTile * kRotTile) k_rotate_gram(RotateGramParams p) {
+  constexpr int NQ = GramLayout<NB>::NQ, NG = GramLayout<NB>::NG;
+  const size_t npix = size_t(p.W) * p.H;
+  const int tiles_x = (p.W + kRotTile - 1) / kRotTile;
+  const int xd = int(blockIdx.x % tiles_x) * kRotTile + int(threadIdx.x % kRotTile);
+  const int yd = int(blockIdx.x / tiles_x) * kRotTile + int(threadIdx.x / kRotTile);
+  if (xd >= p.W || yd >= p.H) return;
+  const size_t t = size_t(yd) * p.W + xd;
+  const float4 *gm = p.gram + size_t(blockIdx.y) * npix * NQ;
+  double sum = 0.0;
+  uint32_t count = 0;
+  for (uint32_t a0 = 0; a0 < p.nangles; a0 += kRotUnroll) {
+    WarpTap tp[kRotUnroll];
+    bool in[kRotUnroll];
+    float4 cv[kRotUnroll][4][NQ];
+#pragma unroll
+    for (int u = 0; u < kRotUnroll; ++u) {
+      const uint32_t a = a0 + u;
+      in[u] = a < p.nangles && warp_tap(p.W, p.H, p.coef[a < p.nangles ? a : 0], xd, yd, tp[u]);
+      if (!in[u]) tp[u] = WarpTap{0, 0, 0, 0, 0.f, 0.f};
+      const int idx[4] = {tp[u].i00, tp[u].i01, tp[u].i10, tp[u].i11};
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) cv[u][c][q] = __ldg(&gm[size_t(idx[c]) * NQ + q]);
+    }
+#pragma unroll
+    for (int u = 0; u < kRotUnroll; ++u) {
+      const uint32_t a = a0 + u;
+      if (a >= p.nangles) break;
+      float v = __int_as_float(0x7fc00000);
+      if (in[u]) {
+        float G[NG];
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          const int q = g / 4, r = g % 4;
+          auto comp = [&](const float4 &f) { return r == 0 ? f.x : r == 1 ? f.y : r == 2 ? f.z : f.w; };
+          G[g] = warp_blend(tp[u].fx, tp[u].fy, comp(cv[u][0][q]), comp(cv[u][1][q]), comp(cv[u][2][q]),
+                            comp(cv[u][3][q]));
+        }
+        v = gram_intensity<NB>(G, p.ecoef + size_t(a) * NB);
+      }
+      if (p.rot_mask) {
+        if (isnan(v)) {
+          v = 0.f;
+        } else {
+          ++count;
+        }
+      }
+      sum += double(v);
+    }
   }
   float r;
   if (p.rot_mask) {

@@ -61,6 +61,9 @@ def workload(name: str, energies=None) -> Workload:
     if name == "headline":
         es = energies or [float(e) for e in np.linspace(270.0, 300.0, 50)]
         return Workload("headline", 256, 512, 512, 4, es, (0.0, 175.0, 5.0), 2.0, 7, "random")
+    if name == "z64":  # the c2 physics on a 64 x 512 x 512 grid: a profiling size (about 3.5 GB on the device)
+        es = energies or [float(e) for e in np.linspace(270.0, 300.0, 50)]
+        return Workload("z64", 64, 512, 512, 4, es, (0.0, 175.0, 5.0), 2.0, 2, "random")
     if name == "small":
         return Workload("small", 16, 64, 64, 2, energies or [284.0, 286.0], (0.0, 150.0, 30.0), 5.0, 3, "random")
     raise ValueError(f"unknown workload {name}")
