@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -170,15 +171,37 @@ struct ZTune {
   float ms = 0.f;
 };
 
+// Device scratch of one request in flight (grow-only).  The plain entry points
+// share the device context's; every serving slot owns one.
+struct Scratch {
+  DeviceBuffer spec, images, avg, params, dc, moments, means, errors, conv, flags, fmean;
+  cudaEvent_t last_use = nullptr;  // completion of the last request that used it
+  int init() {
+    if (!last_use) CYR_CUDA(cudaEventCreateWithFlags(&last_use, cudaEventDisableTiming));
+    return CYR_OK;
+  }
+  void release() {
+    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean})
+      b->release();
+  }
+  size_t bytes() const {
+    size_t n = 0;
+    for (const DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean})
+      n += b->bytes;
+    return n;
+  }
+};
+
 struct DeviceContext {
   int device = -1;
   Profiler prof;
+  std::mutex mu;         // the plain entry points (they share `main`)
+  std::mutex tables_mu;  // twiddles, autotuning results, kernel attributes
   std::map<std::string, ZTune> ztune;  // key: nx,ny,nz,nmat,nvol,morphology
-  std::mutex mu;
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
-  DeviceBuffer spec, images, avg, params, dc, vox_in, out_in, moments, means, errors, conv, flags, fmean;
-  cudaEvent_t last_use = nullptr;  // completion of the last request that used the scratch
+  Scratch main;
+  DeviceBuffer vox_in, out_in;  // host-buffer entry points: morphology and projections
 };
 
 std::mutex g_ctx_mu;
@@ -208,6 +231,7 @@ int get_context(DeviceContext **out) {
 constexpr uint32_t kColsTxY = 8, kColsTxZ = 16;
 
 int setup_attrs(DeviceContext &ctx) {
+  std::lock_guard<std::mutex> lk(ctx.tables_mu);
   if (ctx.attrs_done) return CYR_OK;
   const int smem = int(kFftSmemBudget);
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -231,12 +255,12 @@ int setup_attrs(DeviceContext &ctx) {
   CYR_WARP_Z_ATTR_V(16)
 #undef CYR_WARP_Z_ATTR_V
 #undef CYR_WARP_Z_ATTR
-  CYR_CUDA(cudaEventCreateWithFlags(&ctx.last_use, cudaEventDisableTiming));
   ctx.attrs_done = true;
   return CYR_OK;
 }
 
 int get_twiddles(DeviceContext &ctx, uint32_t n, const float2 **tw) {
+  std::lock_guard<std::mutex> lk(ctx.tables_mu);
   auto it = ctx.twiddles.find(n);
   if (it != ctx.twiddles.end()) {
     *tw = it->second;
@@ -470,6 +494,24 @@ size_t arena_put(std::vector<unsigned char> &a, const T *src, size_t count) {
   return off;
 }
 
+// make_kframe scans 100 000 candidate base angles (as the reference does per
+// call); the frame depends only on k, so it is computed once per k vector.
+KFrame cached_kframe(const Vec3f &k) {
+  static std::mutex mu;
+  static std::map<std::array<uint32_t, 3>, KFrame> cache;
+  std::array<uint32_t, 3> key;
+  std::memcpy(key.data(), &k.x, 4), std::memcpy(key.data() + 1, &k.y, 4), std::memcpy(key.data() + 2, &k.z, 4);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  const KFrame f = make_kframe(k);
+  std::lock_guard<std::mutex> lk(mu);
+  cache.emplace(key, f);
+  return f;
+}
+
 int validate(const cyr_options *o) {
   if (!o) return fail(CYR_ERR_ARGUMENT, "options pointer is null");
   if (o->nx < 2 || o->ny < 2 || o->nz < 1) return fail(CYR_ERR_ARGUMENT, "dimensions must be nx, ny >= 2, nz >= 1");
@@ -521,7 +563,7 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
     for (uint32_t i = 0; i < o->num_k; ++i) ks.push_back({o->k_vectors[3 * i], o->k_vectors[3 * i + 1], o->k_vectors[3 * i + 2]});
   }
   pl.nk = uint32_t(ks.size());
-  for (const Vec3f &k : ks) pl.frames.push_back(make_kframe(k));
+  for (const Vec3f &k : ks) pl.frames.push_back(cached_kframe(k));
   const Vec3f det = o->case_type == 2 ? Vec3f{o->detector[0], o->detector[1], o->detector[2]} : Vec3f{0.f, 0.f, 1.f};
   pl.detector = rotation_between({0.f, 0.f, 1.f}, det);
   // per (k, angle): E angle, rotation, E vector
@@ -775,25 +817,25 @@ EwaldParams ewald_params(const Plan &pl, const cyr_options *o, const unsigned ch
 
 // FIELDS strategy after the moments: field means, packed field spectra, then
 // every energy (in batches) and k from them.
-int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const unsigned char *dp,
+int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan &pl, const unsigned char *dp,
                const float4 *d_vox, float *d_out, cudaStream_t st) {
   const uint32_t nf = num_fields(pl.nmat), npk = pl.npk;
-  CYR_TRY(ctx.fmean.ensure(nf * sizeof(float)));
-  CYR_TRY(ctx.spec.ensure(size_t(npk) * pl.nvox * sizeof(float2)));
-  CYR_TRY(ctx.dc.ensure(size_t(npk) * sizeof(float2)));
-  CYR_TRY(ctx.images.ensure(size_t(pl.ebatch) * image_bytes(pl)));
-  CYR_TRY(ctx.avg.ensure(size_t(pl.ebatch) * pl.npix * sizeof(float)));
-  float2 *spec = ctx.spec.as<float2>();
+  CYR_TRY(sc.fmean.ensure(nf * sizeof(float)));
+  CYR_TRY(sc.spec.ensure(size_t(npk) * pl.nvox * sizeof(float2)));
+  CYR_TRY(sc.dc.ensure(size_t(npk) * sizeof(float2)));
+  CYR_TRY(sc.images.ensure(size_t(pl.ebatch) * image_bytes(pl)));
+  CYR_TRY(sc.avg.ensure(size_t(pl.ebatch) * pl.npix * sizeof(float)));
+  float2 *spec = sc.spec.as<float2>();
   int slot = ctx.prof.begin(kFieldMeans, st);
-  k_field_means<<<1, 128, 0, st>>>(ctx.moments.as<double>(), pl.nmat,
-                                   pl.npix * ((pl.nz + pl.mom_zstep - 1) / pl.mom_zstep), ctx.fmean.as<float>());
+  k_field_means<<<1, 128, 0, st>>>(sc.moments.as<double>(), pl.nmat,
+                                   pl.npix * ((pl.nz + pl.mom_zstep - 1) / pl.mom_zstep), sc.fmean.as<float>());
   ctx.prof.end(slot, st);
   CYR_CUDA(cudaGetLastError());
   FieldParams fp{};
   fp.vox = d_vox;
   fp.nx = pl.nx, fp.ny = pl.ny, fp.nz = pl.nz, fp.nmat = pl.nmat;
   fp.nvox = pl.nvox;
-  fp.mean = ctx.fmean.as<float>();
+  fp.mean = sc.fmean.as<float>();
   if (pl.hanning) {
     fp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
     fp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
@@ -813,13 +855,13 @@ int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const u
   CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st));
   slot = ctx.prof.begin(kDc, st);
   k_dc<<<1, (npk + 31) / 32 * 32, 0, st>>>(spec, npk, pl.nvox, pl.nx, pl.ny, pl.nz, 0, 1 % pl.nz, pl.nz - 1,
-                                           ctx.dc.as<float2>());
+                                           sc.dc.as<float2>());
   ctx.prof.end(slot, st);
   CYR_CUDA(cudaGetLastError());
 
   FieldEwaldParams fe{};
   fe.zspec = spec;
-  fe.zdc = ctx.dc.as<float2>();
+  fe.zdc = sc.dc.as<float2>();
   fe.npk = npk;
   fe.nvox = pl.nvox;
   fe.coef = reinterpret_cast<const float4 *>(dp + pl.off_fcoef);
@@ -835,8 +877,8 @@ int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const u
   fe.qy = reinterpret_cast<const float *>(dp + pl.off_qy);
   fe.qz = reinterpret_cast<const float *>(dp + pl.off_qz);
   fe.nangles = pl.nang;
-  fe.images = ctx.images.as<float>();
-  fe.gram = ctx.images.as<float4>();
+  fe.images = sc.images.as<float>();
+  fe.gram = sc.images.as<float4>();
   const size_t fsmem = size_t(6) * npk * sizeof(float4);
   const unsigned pix_blocks = unsigned((pl.npix + 255) / 256);
   const unsigned fpix_blocks = unsigned((pl.npix + kFieldEwaldThreads - 1) / kFieldEwaldThreads);
@@ -852,14 +894,14 @@ int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const u
     fe.mat = dmat + size_t(k) * pl.nang * 18;
     fe.ecoef = reinterpret_cast<const float *>(dp + pl.off_coef) + size_t(k) * pl.nang * pl.nbasis;
     RotateParams rp{};
-    rp.images = ctx.images.as<float>();
+    rp.images = sc.images.as<float>();
     rp.coef = dwarp + size_t(k) * pl.nang;
     rp.W = W, rp.H = H;
     rp.nangles = pl.nang;
     rp.rot_mask = o->rot_mask;
-    rp.avg = ctx.avg.as<float>();
+    rp.avg = sc.avg.as<float>();
     RotateGramParams rg{};
-    rg.gram = ctx.images.as<float4>();
+    rg.gram = sc.images.as<float4>();
     rg.coef = rp.coef;
     rg.ecoef = fe.ecoef;
     rg.W = W, rg.H = H;
@@ -892,50 +934,51 @@ int run_fields(DeviceContext &ctx, const cyr_options *o, const Plan &pl, const u
       k_fill<<<dim3(pix_blocks, nb), 256, 0, st>>>(dst, pl.npix, fillv, ostride);
       ctx.prof.end(slot, st);
       slot = ctx.prof.begin(kWarp, st);
-      k_warp<<<dim3(pix_blocks, nb), 256, 0, st>>>(ctx.avg.as<float>(), dst, W, H, pl.detector_warp[k], pl.npix,
+      k_warp<<<dim3(pix_blocks, nb), 256, 0, st>>>(sc.avg.as<float>(), dst, W, H, pl.detector_warp[k], pl.npix,
                                                    ostride);
       ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());
     }
   }
-  CYR_CUDA(cudaEventRecord(ctx.last_use, st));
+  CYR_CUDA(cudaEventRecord(sc.last_use, st));
   return CYR_OK;
 }
 
-int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, const float4 *d_vox, float *d_out,
-                cudaStream_t st) {
+int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const float *optical, const float4 *d_vox,
+                float *d_out, cudaStream_t st) {
   Plan pl;
   CYR_TRY(make_plan(o, optical, pl));
   CYR_TRY(setup_attrs(ctx));
+  CYR_TRY(sc.init());
   if (pl.fields && o->strategy == CYR_STRATEGY_AUTO) {
     // AUTO falls back to the per-energy spectra when the field volumes do not fit
     size_t free_b = 0, total_b = 0;
     CYR_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const size_t reusable = ctx.spec.bytes + ctx.images.bytes + ctx.avg.bytes;
+    const size_t reusable = sc.spec.bytes + sc.images.bytes + sc.avg.bytes;
     if (field_bytes(pl) + (size_t(1) << 30) > free_b + reusable) pl.fields = false;
   }
   // scratch (grow-only); wait for the previous user of the scratch
-  CYR_CUDA(cudaStreamWaitEvent(st, ctx.last_use, 0));
-  CYR_TRY(ctx.errors.ensure(sizeof(unsigned)));
-  CYR_CUDA(cudaMemsetAsync(ctx.errors.ptr, 0, sizeof(unsigned), st));
+  CYR_CUDA(cudaStreamWaitEvent(st, sc.last_use, 0));
+  CYR_TRY(sc.errors.ensure(sizeof(unsigned)));
+  CYR_CUDA(cudaMemsetAsync(sc.errors.ptr, 0, sizeof(unsigned), st));
   if (!pl.fields) {
-    CYR_TRY(ctx.spec.ensure(pl.nvol * pl.vstride * sizeof(float2)));
-    CYR_TRY(ctx.images.ensure(image_bytes(pl)));
-    CYR_TRY(ctx.avg.ensure(pl.npix * sizeof(float)));
-    CYR_TRY(ctx.dc.ensure(8 * sizeof(float2)));
+    CYR_TRY(sc.spec.ensure(pl.nvol * pl.vstride * sizeof(float2)));
+    CYR_TRY(sc.images.ensure(image_bytes(pl)));
+    CYR_TRY(sc.avg.ensure(pl.npix * sizeof(float)));
+    CYR_TRY(sc.dc.ensure(8 * sizeof(float2)));
   }
-  CYR_TRY(ctx.params.ensure(pl.arena.size()));
-  CYR_CUDA(cudaMemcpyAsync(ctx.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
-  const unsigned char *dp = ctx.params.as<unsigned char>();
+  CYR_TRY(sc.params.ensure(pl.arena.size()));
+  CYR_CUDA(cudaMemcpyAsync(sc.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
+  const unsigned char *dp = sc.params.as<unsigned char>();
   // volume moments of the morphology -> mean of every tensor entry, per energy
-  CYR_TRY(ctx.moments.ensure(size_t(pl.nmat) * kMoments * sizeof(double)));
-  CYR_TRY(ctx.means.ensure(size_t(pl.ne) * 6 * sizeof(float2)));
-  CYR_CUDA(cudaMemsetAsync(ctx.moments.ptr, 0, size_t(pl.nmat) * kMoments * sizeof(double), st));
+  CYR_TRY(sc.moments.ensure(size_t(pl.nmat) * kMoments * sizeof(double)));
+  CYR_TRY(sc.means.ensure(size_t(pl.ne) * 6 * sizeof(float2)));
+  CYR_CUDA(cudaMemsetAsync(sc.moments.ptr, 0, size_t(pl.nmat) * kMoments * sizeof(double), st));
   // Euler morphologies are converted once per request to the trigonometry-free vector form
   const bool convert = o->morphology_type == 0 && !pl.fields;
-  CYR_TRY(ctx.flags.ensure(sizeof(unsigned)));
-  CYR_CUDA(cudaMemsetAsync(ctx.flags.ptr, 0, sizeof(unsigned), st));
-  if (convert) CYR_TRY(ctx.conv.ensure(pl.nvox * pl.nmat * sizeof(float4)));
+  CYR_TRY(sc.flags.ensure(sizeof(unsigned)));
+  CYR_CUDA(cudaMemsetAsync(sc.flags.ptr, 0, sizeof(unsigned), st));
+  if (convert) CYR_TRY(sc.conv.ensure(pl.nvox * pl.nmat * sizeof(float4)));
   {
     MomentParams mp{};
     mp.vox = d_vox;
@@ -946,11 +989,11 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       mp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
       mp.hann_z = reinterpret_cast<const float *>(dp + pl.off_hz);
     }
-    mp.out = ctx.moments.as<double>();
-    mp.conv = convert ? ctx.conv.as<float4>() : nullptr;
+    mp.out = sc.moments.as<double>();
+    mp.conv = convert ? sc.conv.as<float4>() : nullptr;
     // the conversion needs every voxel; the means alone need only a subsample of planes
     mp.zstep = convert ? 1u : pl.mom_zstep;
-    mp.neg = ctx.flags.as<unsigned>();
+    mp.neg = sc.flags.as<unsigned>();
     int nsm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx.device));
     const dim3 grid(uint32_t(std::max<size_t>(1, std::min<size_t>((pl.nvox + 255) / 256, size_t(nsm) * 8))), pl.nmat);
@@ -961,18 +1004,18 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       k_moments<1><<<grid, 256, 0, st>>>(mp);
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
-    if (pl.fields) return run_fields(ctx, o, pl, dp, d_vox, d_out, st);
+    if (pl.fields) return run_fields(ctx, sc, o, pl, dp, d_vox, d_out, st);
     slot = ctx.prof.begin(kMeans, st);
-    k_entry_means<<<1, 64, 0, st>>>(ctx.moments.as<double>(), pl.nmat, pl.nvox,
+    k_entry_means<<<1, 64, 0, st>>>(sc.moments.as<double>(), pl.nmat, pl.nvox,
                                     reinterpret_cast<const MaterialConsts *>(dp + pl.off_mc), pl.ne,
-                                    ctx.means.as<float2>());
+                                    sc.means.as<float2>());
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
   }
-  float2 *spec = ctx.spec.as<float2>();
-  float2 *dc = ctx.dc.as<float2>();
-  float *images = ctx.images.as<float>();
-  float *avg = ctx.avg.as<float>();
+  float2 *spec = sc.spec.as<float2>();
+  float2 *dc = sc.dc.as<float2>();
+  float *images = sc.images.as<float>();
+  float *avg = sc.avg.as<float>();
   const MaterialConsts *dmc = reinterpret_cast<const MaterialConsts *>(dp + pl.off_mc);
 
   BuildParams bp{};
@@ -981,8 +1024,8 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   bp.nvox = pl.nvox;
   bp.morphology = o->morphology_type;
   bp.out = spec;
-  bp.conv = convert ? ctx.conv.as<float4>() : nullptr;
-  bp.neg = ctx.flags.as<unsigned>();
+  bp.conv = convert ? sc.conv.as<float4>() : nullptr;
+  bp.neg = sc.flags.as<unsigned>();
   if (pl.hanning) {
     bp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
     bp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
@@ -992,7 +1035,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
   CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
   const uint32_t build_blocks = uint32_t(std::min<size_t>((pl.nvox + 255) / 256, size_t(sms) * 8));
   EwaldParams ep = ewald_params(pl, o, dp, spec, dc, images);
-  ep.errors = ctx.errors.as<unsigned>();
+  ep.errors = sc.errors.as<unsigned>();
   FftAxis az{};
   if (pl.pruned) CYR_TRY(make_axis(ctx, pl.nz, az));
   // spectra of the current BuildParams (nvol volumes): pruned (build + z FFT
@@ -1041,8 +1084,15 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
         char key[96];
         std::snprintf(key, sizeof key, "%u,%u,%u,%u,%u,%u", pl.nx, pl.ny, pl.nz, pl.nmat, bp.nvol,
                       o->morphology_type);
-        auto it = ctx.ztune.find(key);
-        if (it == ctx.ztune.end() && pl.zcands.size() > 1 && !ctx.prof.active) {
+        ZTune tuned;
+        bool have_tuned;
+        {
+          std::lock_guard<std::mutex> lk(ctx.tables_mu);
+          auto it = ctx.ztune.find(key);
+          have_tuned = it != ctx.ztune.end();
+          if (have_tuned) tuned = it->second;
+        }
+        if (!have_tuned && pl.zcands.size() > 1 && !ctx.prof.active) {
           // autotune: time every candidate once on this energy; the last one's
           // output stays in `spec` and is used
           std::vector<cudaEvent_t> ev(2 * pl.zcands.size());
@@ -1062,12 +1112,15 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
             if (ms < best.ms) best = pl.zcands[c], best.ms = ms;
           }
           for (auto &e : ev) cudaEventDestroy(e);
-          ctx.ztune[key] = best;
+          {
+            std::lock_guard<std::mutex> lk(ctx.tables_mu);
+            ctx.ztune[key] = best;
+          }
           launch_warp(best);  // the kept output must come from a full, ordered launch of the chosen form
         } else {
           ZTune cfg;
-          if (it != ctx.ztune.end()) {
-            cfg = it->second;
+          if (have_tuned) {
+            cfg = tuned;
           } else {
             cfg.stage = pl.zstage;
             cfg.tx = pl.ztx;
@@ -1124,7 +1177,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       // tensor entries once per energy: xx xy xz yy yz [zz]
       bp.mode = 0;
       bp.nvol = pl.nvol;
-      bp.mean = ctx.means.as<float2>() + size_t(e) * 6;
+      bp.mean = sc.means.as<float2>() + size_t(e) * 6;
       CYR_TRY(spectra(mce));
     }
     for (uint32_t k = 0; k < pl.nk; ++k) {
@@ -1150,7 +1203,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
           bp.mode = 1;
           bp.nvol = 3;
           bp.material_frame = 1;
-          bp.mean = ctx.means.as<float2>() + size_t(e) * 6;
+          bp.mean = sc.means.as<float2>() + size_t(e) * 6;
           for (int c = 0; c < 3; ++c) bp.E[c] = pl.evec[ka * 3 + c];
           std::memcpy(bp.Rm, pl.rmats[ka].m, sizeof bp.Rm);
           CYR_TRY(spectra(mce));
@@ -1200,7 +1253,7 @@ int run_request(DeviceContext &ctx, const cyr_options *o, const float *optical, 
       CYR_CUDA(cudaGetLastError());
     }
   }
-  CYR_CUDA(cudaEventRecord(ctx.last_use, st));
+  CYR_CUDA(cudaEventRecord(sc.last_use, st));
   return CYR_OK;
 }
 
@@ -1252,7 +1305,7 @@ int cyr_plan_info(const cyr_options *opt, uint32_t *info, uint32_t n) {
 int cyr_tuning_report(char *buf, size_t len) {
   DeviceContext *ctx = nullptr;
   CYR_TRY(get_context(&ctx));
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::mutex> lk(ctx->tables_mu);
   std::string r;
   for (const auto &kv : ctx->ztune) {
     char line[160];
@@ -1273,10 +1326,10 @@ int cyr_device_errors(uint32_t *count) {
   CYR_TRY(get_context(&ctx));
   std::lock_guard<std::mutex> lk(ctx->mu);
   *count = 0;
-  if (!ctx->errors.ptr) return CYR_OK;
+  if (!ctx->main.errors.ptr) return CYR_OK;
   CYR_CUDA(cudaDeviceSynchronize());
   unsigned h = 0;
-  CYR_CUDA(cudaMemcpy(&h, ctx->errors.ptr, sizeof h, cudaMemcpyDeviceToHost));
+  CYR_CUDA(cudaMemcpy(&h, ctx->main.errors.ptr, sizeof h, cudaMemcpyDeviceToHost));
   *count = h;
   return CYR_OK;
 }
@@ -1286,17 +1339,7 @@ int cyr_release_scratch(void) {
   CYR_TRY(get_context(&ctx));
   std::lock_guard<std::mutex> lk(ctx->mu);
   CYR_CUDA(cudaDeviceSynchronize());
-  ctx->spec.release();
-  ctx->images.release();
-  ctx->avg.release();
-  ctx->params.release();
-  ctx->dc.release();
-  ctx->moments.release();
-  ctx->means.release();
-  ctx->errors.release();
-  ctx->conv.release();
-  ctx->flags.release();
-  ctx->fmean.release();
+  ctx->main.release();
   ctx->vox_in.release();
   ctx->out_in.release();
   return CYR_OK;
@@ -1308,7 +1351,7 @@ int cyr_simulate_device(const cyr_options *opt, const float *optical, const void
   DeviceContext *ctx = nullptr;
   CYR_TRY(get_context(&ctx));
   std::lock_guard<std::mutex> lk(ctx->mu);
-  return run_request(*ctx, opt, optical, static_cast<const float4 *>(d_voxels), d_projection,
+  return run_request(*ctx, ctx->main, opt, optical, static_cast<const float4 *>(d_voxels), d_projection,
                      static_cast<cudaStream_t>(stream));
 }
 
@@ -1335,7 +1378,7 @@ static int cuda_main_impl(const cyr_options *opt, const float *optical, const fl
       rc = fail(CYR_ERR_CUDA, "voxel upload failed: %s", cudaGetErrorString(cudaGetLastError()));
       break;
     }
-    rc = run_request(*ctx, &o, optical, ctx->vox_in.as<float4>(), ctx->out_in.as<float>(), st);
+    rc = run_request(*ctx, ctx->main, &o, optical, ctx->vox_in.as<float4>(), ctx->out_in.as<float>(), st);
     if (rc != CYR_OK) break;
     if (cudaMemcpyAsync(projection, ctx->out_in.ptr, out_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
       rc = fail(CYR_ERR_CUDA, "projection download failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -1347,7 +1390,7 @@ static int cuda_main_impl(const cyr_options *opt, const float *optical, const fl
       break;
     }
     unsigned errs = 0;
-    if (cudaMemcpy(&errs, ctx->errors.ptr, sizeof errs, cudaMemcpyDeviceToHost) == cudaSuccess && errs != 0)
+    if (cudaMemcpy(&errs, ctx->main.errors.ptr, sizeof errs, cudaMemcpyDeviceToHost) == cudaSuccess && errs != 0)
       rc = fail(CYR_ERR_CUDA, "%u detector pixels needed z planes outside the kept range", errs);
   } while (false);
   cudaStreamDestroy(st);
@@ -1375,16 +1418,16 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
   CYR_TRY(setup_attrs(*ctx));
   const size_t vox_bytes = pl.nvox * pl.nmat * sizeof(float4);
   CYR_TRY(ctx->vox_in.ensure(vox_bytes));
-  CYR_TRY(ctx->spec.ensure(3 * pl.nvox * sizeof(float2)));
-  CYR_TRY(ctx->params.ensure(pl.arena.size()));
+  CYR_TRY(ctx->main.spec.ensure(3 * pl.nvox * sizeof(float2)));
+  CYR_TRY(ctx->main.params.ensure(pl.arena.size()));
   cudaStream_t st = nullptr;
   CYR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   int rc = CYR_OK;
   do {
-    cudaStreamWaitEvent(st, ctx->last_use, 0);
-    cudaMemcpyAsync(ctx->params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st);
+    cudaStreamWaitEvent(st, ctx->main.last_use, 0);
+    cudaMemcpyAsync(ctx->main.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(ctx->vox_in.ptr, voxels, vox_bytes, cudaMemcpyHostToDevice, st);
-    const unsigned char *dp = ctx->params.as<unsigned char>();
+    const unsigned char *dp = ctx->main.params.as<unsigned char>();
     BuildParams bp{};
     bp.vox = ctx->vox_in.as<float4>();
     bp.nx = pl.nx, bp.ny = pl.ny, bp.nz = pl.nz, bp.nmat = pl.nmat;
@@ -1392,7 +1435,7 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
     bp.morphology = opt->morphology_type;
     bp.mode = 1;
     bp.nvol = 3;
-    bp.out = ctx->spec.as<float2>();
+    bp.out = ctx->main.spec.as<float2>();
     bp.material_frame = pl.material_frame ? 1u : 0u;
     // the debug path rotates E by EAngle radians about k (src/cudaMain.cu:1716-1721)
     const Mat3f R = e_rotation(pl.frames[0], eangle);
@@ -1414,10 +1457,10 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
       break;
     }
     const size_t cb = pl.nvox * sizeof(float2);
-    cudaMemcpyAsync(px, ctx->spec.as<float2>(), cb, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(py, ctx->spec.as<float2>() + pl.nvox, cb, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(pz, ctx->spec.as<float2>() + 2 * pl.nvox, cb, cudaMemcpyDeviceToHost, st);
-    cudaEventRecord(ctx->last_use, st);
+    cudaMemcpyAsync(px, ctx->main.spec.as<float2>(), cb, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(py, ctx->main.spec.as<float2>() + pl.nvox, cb, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(pz, ctx->main.spec.as<float2>() + 2 * pl.nvox, cb, cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(ctx->main.last_use, st);
     const cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = fail(CYR_ERR_CUDA, "polarization failed: %s", cudaGetErrorString(e));
   } while (false);

@@ -560,12 +560,11 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
 // (contiguous reads, each stage's strided stores) and of the TX-column tile
 // copies (TX = 2..16, line_stride below): no half-warp access puts two lanes
 // on one bank.  A bijection on [0, N), so lines need no padding.
-__device__ __forceinline__ uint32_t swz(uint32_t p) {
-  const uint32_t h = p >> 4;
-  const uint32_t x = ((h & 1u) ? 10u : 0u) ^ ((h & 2u) ? 15u : 0u) ^ ((h & 4u) ? 12u : 0u) ^
-                     ((h & 8u) ? 3u : 0u) ^ ((h & 16u) ? 12u : 0u);
-  return p ^ x;
+__host__ __device__ constexpr uint32_t swz_mask(uint32_t h) {  // h = p >> 4
+  return ((h & 1u) ? 10u : 0u) ^ ((h & 2u) ? 15u : 0u) ^ ((h & 4u) ? 12u : 0u) ^ ((h & 8u) ? 3u : 0u) ^
+         ((h & 16u) ? 12u : 0u);
 }
+__device__ __forceinline__ uint32_t swz(uint32_t p) { return p ^ swz_mask(p >> 4); }
 // Stride between the lines of TX interleaved columns: congruent to 16 / TX
 // (1 for TX >= 16) modulo 16, so a half-warp touching TX columns x (16 / TX)
 // consecutive positions hits 16 distinct 8-byte banks.
@@ -633,9 +632,12 @@ __device__ __forceinline__ void warp_stage(float2 (&v)[V], float2 *line, const f
 #pragma unroll
       for (int r = 0; r < R; ++r) v[q + r * B] = w[r];  // position j + r N/R: natural order
     } else {
+      // base and r NS occupy disjoint bits, and swz_mask is linear over GF(2):
+      // swz(base + r NS) = (base + r NS) ^ swz_mask(base >> 4) ^ swz_mask(r NS >> 4)
       const uint32_t base = (j / NS) * NS * R + k;
+      const uint32_t xb = swz_mask(base >> 4);
 #pragma unroll
-      for (int r = 0; r < R; ++r) line[swz(base + r * NS)] = w[r];
+      for (int r = 0; r < R; ++r) line[(base + r * NS) ^ xb ^ swz_mask((uint32_t(r) * NS) >> 4)] = w[r];
     }
   }
   if (!LAST) {
