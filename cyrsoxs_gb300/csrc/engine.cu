@@ -29,6 +29,12 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -105,21 +111,34 @@ uint32_t fft_lines_per_block(uint32_t n) {
 // ---------------------------------------------------------------------------
 // Per-device context: cached twiddle tables and grow-only scratch.
 // ---------------------------------------------------------------------------
+// Grow-only device buffer.  With `stream` set (serving slots) it allocates
+// and frees stream-ordered, so growing one slot's buffer does not stall the
+// others; `generation` counts reallocations (captured graphs hold pointers).
 struct DeviceBuffer {
   void *ptr = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t *generation = nullptr;
   int ensure(size_t need) {
     if (need <= bytes) return CYR_OK;
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    bytes = 0;
+    release();
     if (need == 0) return CYR_OK;
-    CYR_CUDA(cudaMalloc(&ptr, need));
+    if (stream)
+      CYR_CUDA(cudaMallocAsync(&ptr, need, stream));
+    else
+      CYR_CUDA(cudaMalloc(&ptr, need));
     bytes = need;
+    if (generation) ++*generation;
     return CYR_OK;
   }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      if (stream)
+        cudaFreeAsync(ptr, stream);
+      else
+        cudaFree(ptr);
+      if (generation) ++*generation;
+    }
     ptr = nullptr;
     bytes = 0;
   }
@@ -176,9 +195,15 @@ struct ZTune {
 struct Scratch {
   DeviceBuffer spec, images, avg, params, dc, moments, means, errors, conv, flags, fmean;
   cudaEvent_t last_use = nullptr;  // completion of the last request that used it
+  uint64_t generation = 0;         // bumped by every (re)allocation of a buffer above
   int init() {
     if (!last_use) CYR_CUDA(cudaEventCreateWithFlags(&last_use, cudaEventDisableTiming));
     return CYR_OK;
+  }
+  // serving slots: stream-ordered allocations on `st`
+  void bind(cudaStream_t st) {
+    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean})
+      b->stream = st, b->generation = &generation;
   }
   void release() {
     for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean})
@@ -944,13 +969,23 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   return CYR_OK;
 }
 
+// How a request is enqueued.  host_arena: pinned copy of the parameter arena
+// that outlives the call (required while capturing a graph: the upload node
+// reads it at every replay); capturing: no host synchronisation, no device
+// queries and no autotuning (a warm request of the same shape ran before).
+struct RunMode {
+  unsigned char *host_arena = nullptr;
+  size_t host_arena_bytes = 0;
+  bool capturing = false;
+};
+
 int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const float *optical, const float4 *d_vox,
-                float *d_out, cudaStream_t st) {
+                float *d_out, cudaStream_t st, const RunMode &mode = RunMode()) {
   Plan pl;
   CYR_TRY(make_plan(o, optical, pl));
   CYR_TRY(setup_attrs(ctx));
   CYR_TRY(sc.init());
-  if (pl.fields && o->strategy == CYR_STRATEGY_AUTO) {
+  if (pl.fields && o->strategy == CYR_STRATEGY_AUTO && !mode.capturing) {
     // AUTO falls back to the per-energy spectra when the field volumes do not fit
     size_t free_b = 0, total_b = 0;
     CYR_CUDA(cudaMemGetInfo(&free_b, &total_b));
@@ -958,7 +993,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
     if (field_bytes(pl) + (size_t(1) << 30) > free_b + reusable) pl.fields = false;
   }
   // scratch (grow-only); wait for the previous user of the scratch
-  CYR_CUDA(cudaStreamWaitEvent(st, sc.last_use, 0));
+  if (!mode.capturing) CYR_CUDA(cudaStreamWaitEvent(st, sc.last_use, 0));
   CYR_TRY(sc.errors.ensure(sizeof(unsigned)));
   CYR_CUDA(cudaMemsetAsync(sc.errors.ptr, 0, sizeof(unsigned), st));
   if (!pl.fields) {
@@ -968,7 +1003,13 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
     CYR_TRY(sc.dc.ensure(8 * sizeof(float2)));
   }
   CYR_TRY(sc.params.ensure(pl.arena.size()));
-  CYR_CUDA(cudaMemcpyAsync(sc.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
+  if (mode.host_arena) {
+    if (pl.arena.size() > mode.host_arena_bytes) return fail(CYR_ERR_ARGUMENT, "parameter arena exceeds its host buffer");
+    std::memcpy(mode.host_arena, pl.arena.data(), pl.arena.size());
+    CYR_CUDA(cudaMemcpyAsync(sc.params.ptr, mode.host_arena, pl.arena.size(), cudaMemcpyHostToDevice, st));
+  } else {
+    CYR_CUDA(cudaMemcpyAsync(sc.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
+  }
   const unsigned char *dp = sc.params.as<unsigned char>();
   // volume moments of the morphology -> mean of every tensor entry, per energy
   CYR_TRY(sc.moments.ensure(size_t(pl.nmat) * kMoments * sizeof(double)));
@@ -1092,7 +1133,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
           have_tuned = it != ctx.ztune.end();
           if (have_tuned) tuned = it->second;
         }
-        if (!have_tuned && pl.zcands.size() > 1 && !ctx.prof.active) {
+        if (!have_tuned && pl.zcands.size() > 1 && !ctx.prof.active && !mode.capturing) {
           // autotune: time every candidate once on this energy; the last one's
           // output stays in `spec` and is used
           std::vector<cudaEvent_t> ev(2 * pl.zcands.size());
@@ -1257,6 +1298,269 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
   return CYR_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Serving engine: continuous batching of simulation requests on one GPU.
+//
+// A worker thread owns S slots.  Each slot has its own stream, its own
+// request scratch (stream-ordered allocations) and staging buffers, so the
+// requests in different slots overlap on the device.  Requests wait in a FIFO
+// queue and are admitted as soon as a slot is free and their device footprint
+// (request_bytes + staging) fits in the HBM budget next to the requests in
+// flight; completion is detected with one event per slot.  Optionally a slot
+// replays a CUDA graph of a request signature it has already run (the same
+// options and input pointers; the optical constants travel in the parameter
+// arena, which each replay rewrites in the slot's pinned host copy).
+// ---------------------------------------------------------------------------
+using Clock = std::chrono::steady_clock;
+
+struct ServerRequest {
+  uint64_t id = 0;
+  cyr_options opt{};
+  std::vector<float> energies, kvecs, optical;
+  const float *h_vox = nullptr;  // host buffers (caller-owned until the request is done)
+  float *h_out = nullptr;
+  const float4 *d_vox = nullptr;  // or device buffers
+  float *d_out = nullptr;
+  size_t vox_bytes = 0, out_bytes = 0, footprint = 0;
+  std::string key;  // graph signature
+  int status = -1;  // -1 queued or running, else a CYR_* code
+  std::string error;
+  Clock::time_point t_submit, t_start, t_done;
+};
+
+struct GraphEntry {
+  cudaGraphExec_t exec = nullptr;
+  uint64_t generation = 0;
+};
+
+struct Slot {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  Scratch sc;
+  DeviceBuffer vox, out;  // staging for host-buffer requests
+  unsigned char *host_arena = nullptr;
+  size_t host_arena_bytes = 0;
+  unsigned *host_errors = nullptr;  // pinned copy of the request's device error counter
+  std::shared_ptr<ServerRequest> req;
+  std::map<std::string, GraphEntry> graphs;
+  std::map<std::string, uint64_t> warm;  // signature -> scratch generation after its last uncaptured run
+  uint64_t generation() const { return sc.generation; }
+};
+
+struct Server {
+  DeviceContext *ctx = nullptr;
+  int device = 0;
+  std::vector<std::unique_ptr<Slot>> slots;
+  size_t budget = 0, in_use = 0;
+  bool graphs = false;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<std::shared_ptr<ServerRequest>> queue;
+  std::map<uint64_t, std::shared_ptr<ServerRequest>> requests;
+  uint64_t next_id = 1;
+  bool stop = false;
+  std::atomic<uint64_t> completed{0}, failed{0}, replays{0}, captures{0};
+  std::thread worker;
+};
+
+// Host planning for one request: resolve the AUTO strategy (so a signature
+// always means the same launch sequence) and compute its footprint.
+int plan_request(ServerRequest &r) {
+  Plan pl;
+  CYR_TRY(make_plan(&r.opt, r.optical.data(), pl));
+  if (r.opt.strategy == CYR_STRATEGY_AUTO) r.opt.strategy = pl.fields ? CYR_STRATEGY_FIELDS : CYR_STRATEGY_PER_ENERGY;
+  r.footprint = request_bytes(pl) + (r.h_vox ? r.vox_bytes + r.out_bytes : 0);
+  char head[256];
+  std::snprintf(head, sizeof head, "%u,%u,%u,%u,%u,%a,%a,%a,%a,%u,%u,%u,%u,%u,%u,%u,%u,%u,%u,%u,%a,%a,%a|%p|%p|",
+                r.opt.nx, r.opt.ny, r.opt.nz, r.opt.num_material, r.opt.num_energies, double(r.opt.start_angle),
+                double(r.opt.end_angle), double(r.opt.increment_angle), double(r.opt.phys_size), r.opt.case_type,
+                r.opt.num_k, r.opt.morphology_type, r.opt.ewald_interpolation, r.opt.windowing,
+                r.opt.scatter_approach, r.opt.algorithm, r.opt.rot_mask, r.opt.reference_frame, r.opt.strategy,
+                r.h_vox ? 1u : 0u, double(r.opt.detector[0]), double(r.opt.detector[1]), double(r.opt.detector[2]),
+                static_cast<const void *>(r.d_vox), static_cast<void *>(r.d_out));
+  r.key = head;
+  for (float e : r.energies) r.key += std::to_string(e) + ",";
+  for (float k : r.kvecs) r.key += std::to_string(k) + ",";
+  return CYR_OK;
+}
+
+// Enqueues request r on slot sl (worker thread).
+int start_request(Server &S, Slot &sl, ServerRequest &r) {
+  cudaStream_t st = sl.stream;
+  const float4 *d_vox = r.d_vox;
+  float *d_out = r.d_out;
+  if (r.h_vox) {
+    CYR_TRY(sl.vox.ensure(r.vox_bytes));
+    CYR_TRY(sl.out.ensure(r.out_bytes));
+    CYR_CUDA(cudaMemcpyAsync(sl.vox.ptr, r.h_vox, r.vox_bytes, cudaMemcpyHostToDevice, st));
+    d_vox = sl.vox.as<float4>();
+    d_out = sl.out.as<float>();
+  }
+  Plan pl;
+  CYR_TRY(make_plan(&r.opt, r.optical.data(), pl));
+  if (pl.arena.size() > sl.host_arena_bytes) {
+    if (sl.host_arena) {
+      CYR_CUDA(cudaStreamSynchronize(st));
+      cudaFreeHost(sl.host_arena);
+      sl.host_arena = nullptr;
+    }
+    for (auto &kv : sl.graphs) cudaGraphExecDestroy(kv.second.exec);  // their upload nodes read the old copy
+    sl.graphs.clear();
+    sl.host_arena_bytes = std::max<size_t>(pl.arena.size(), 64 * 1024);
+    CYR_CUDA(cudaMallocHost(&sl.host_arena, sl.host_arena_bytes));
+  }
+  RunMode mode;
+  mode.host_arena = sl.host_arena;
+  mode.host_arena_bytes = sl.host_arena_bytes;
+  auto git = S.graphs ? sl.graphs.find(r.key) : sl.graphs.end();
+  if (git != sl.graphs.end() && git->second.generation == sl.generation()) {
+    std::memcpy(sl.host_arena, pl.arena.data(), pl.arena.size());
+    CYR_CUDA(cudaGraphLaunch(git->second.exec, st));
+    ++S.replays;
+  } else {
+    auto wit = sl.warm.find(r.key);
+    if (S.graphs && wit != sl.warm.end() && wit->second == sl.generation()) {
+      // same signature ran on these buffers: capture (nothing is allocated) and replay
+      if (git != sl.graphs.end()) {
+        cudaGraphExecDestroy(git->second.exec);
+        sl.graphs.erase(git);
+      }
+      mode.capturing = true;
+      CYR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      const int rc = run_request(*S.ctx, sl.sc, &r.opt, r.optical.data(), d_vox, d_out, st, mode);
+      cudaGraph_t g = nullptr;
+      const cudaError_t ec = cudaStreamEndCapture(st, &g);
+      if (rc != CYR_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (ec != cudaSuccess) return fail(CYR_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+      GraphEntry ge;
+      const cudaError_t ei = cudaGraphInstantiate(&ge.exec, g, 0);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) return fail(CYR_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ei));
+      ge.generation = sl.generation();
+      CYR_CUDA(cudaGraphLaunch(ge.exec, st));
+      sl.graphs[r.key] = ge;
+      ++S.captures;
+    } else {
+      CYR_TRY(run_request(*S.ctx, sl.sc, &r.opt, r.optical.data(), d_vox, d_out, st, mode));
+      sl.warm[r.key] = sl.generation();
+    }
+  }
+  CYR_CUDA(cudaMemcpyAsync(sl.host_errors, sl.sc.errors.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  if (r.h_out) CYR_CUDA(cudaMemcpyAsync(r.h_out, d_out, r.out_bytes, cudaMemcpyDeviceToHost, st));
+  CYR_CUDA(cudaEventRecord(sl.done, st));
+  return CYR_OK;
+}
+
+void finish_request(Server &S, Slot &sl, int status, const std::string &err) {
+  std::shared_ptr<ServerRequest> r = sl.req;
+  sl.req.reset();
+  std::lock_guard<std::mutex> lk(S.mu);
+  r->t_done = Clock::now();
+  r->status = status;
+  r->error = err;
+  S.in_use -= std::min(S.in_use, r->footprint);
+  if (status == CYR_OK)
+    ++S.completed;
+  else
+    ++S.failed;
+  S.cv_done.notify_all();
+}
+
+void server_loop(Server *Sp) {
+  Server &S = *Sp;
+  cudaSetDevice(S.device);
+  for (;;) {
+    bool progress = false;
+    // completions
+    for (auto &slp : S.slots) {
+      Slot &sl = *slp;
+      if (!sl.req) continue;
+      const cudaError_t q = cudaEventQuery(sl.done);
+      if (q == cudaErrorNotReady) continue;
+      progress = true;
+      if (q != cudaSuccess) {
+        finish_request(S, sl, CYR_ERR_CUDA, std::string("request failed on the device: ") + cudaGetErrorString(q));
+      } else if (*sl.host_errors != 0) {
+        char m[128];
+        std::snprintf(m, sizeof m, "%u detector pixels needed z planes outside the kept range", *sl.host_errors);
+        finish_request(S, sl, CYR_ERR_CUDA, m);
+      } else {
+        finish_request(S, sl, CYR_OK, "");
+      }
+    }
+    // admissions (FIFO): a free slot and room in the budget; a request larger
+    // than the whole budget runs alone
+    for (;;) {
+      std::shared_ptr<ServerRequest> r;
+      Slot *free_slot = nullptr;
+      bool any_active = false;
+      for (auto &slp : S.slots) {
+        if (slp->req)
+          any_active = true;
+        else if (!free_slot)
+          free_slot = slp.get();
+      }
+      {
+        std::lock_guard<std::mutex> lk(S.mu);
+        if (S.queue.empty() || !free_slot) break;
+        r = S.queue.front();
+        if (any_active && S.in_use + r->footprint > S.budget) break;
+        S.queue.pop_front();
+        S.in_use += r->footprint;
+        r->t_start = Clock::now();
+      }
+      progress = true;
+      free_slot->req = r;
+      const int rc = start_request(S, *free_slot, *r);
+      if (rc != CYR_OK) {
+        const std::string err = g_error;
+        cudaStreamSynchronize(free_slot->stream);  // let whatever was enqueued finish before the slot is reused
+        cudaGetLastError();
+        finish_request(S, *free_slot, rc, err);
+      }
+    }
+    bool active = false;
+    for (auto &slp : S.slots) active = active || slp->req != nullptr;
+    std::unique_lock<std::mutex> lk(S.mu);
+    if (S.stop && S.queue.empty() && !active) break;
+    if (!active && S.queue.empty()) {
+      S.cv_work.wait(lk, [&] { return S.stop || !S.queue.empty(); });
+    } else if (!progress) {
+      // requests in flight: poll their events again shortly
+      S.cv_work.wait_for(lk, std::chrono::microseconds(20));
+    }
+  }
+}
+
+int server_destroy(Server *S) {
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->cv_work.notify_all();
+  if (S->worker.joinable()) S->worker.join();
+  cudaSetDevice(S->device);
+  for (auto &slp : S->slots) {
+    Slot &sl = *slp;
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    for (auto &kv : sl.graphs) cudaGraphExecDestroy(kv.second.exec);
+    sl.sc.release();
+    sl.vox.release();
+    sl.out.release();
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    if (sl.host_arena) cudaFreeHost(sl.host_arena);
+    if (sl.host_errors) cudaFreeHost(sl.host_errors);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.sc.last_use) cudaEventDestroy(sl.sc.last_use);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+  }
+  delete S;
+  return CYR_OK;
+}
 }  // namespace
 }  // namespace cyr
 
@@ -1543,6 +1847,132 @@ int cyr_warp_affine_device(const float *d_src, float *d_dst, int width, int heig
       d_src, d_dst, width, height, WarpCoef{w.a00, w.a01, w.a02, w.a10, w.a11, w.a12});
   CYR_CUDA(cudaGetLastError());
   return CYR_OK;
+}
+
+}  // extern "C"
+
+
+// ---------------------------------------------------------------------------
+// Serving C ABI
+// ---------------------------------------------------------------------------
+struct cyr_server {
+  cyr::Server *impl;
+};
+
+extern "C" {
+
+int cyr_server_create(uint32_t slots, size_t hbm_budget, uint32_t flags, cyr_server **out) {
+  if (!out) return fail(CYR_ERR_ARGUMENT, "out pointer is null");
+  if (slots < 1 || slots > 64) return fail(CYR_ERR_ARGUMENT, "slots must be in [1, 64]");
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  CYR_TRY(setup_attrs(*ctx));
+  std::unique_ptr<Server> S(new Server);
+  S->ctx = ctx;
+  S->device = ctx->device;
+  S->graphs = (flags & CYR_SERVER_GRAPHS) != 0;
+  if (hbm_budget == 0) {
+    size_t free_b = 0, total_b = 0;
+    CYR_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    hbm_budget = free_b / 100 * 85;
+  }
+  S->budget = hbm_budget;
+  for (uint32_t i = 0; i < slots; ++i) {
+    std::unique_ptr<Slot> sl(new Slot);
+    CYR_CUDA(cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking));
+    CYR_CUDA(cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming));
+    CYR_CUDA(cudaMallocHost(&sl->host_errors, sizeof(unsigned)));
+    *sl->host_errors = 0;
+    sl->sc.bind(sl->stream);
+    sl->vox.stream = sl->out.stream = sl->stream;
+    sl->vox.generation = sl->out.generation = &sl->sc.generation;
+    CYR_TRY(sl->sc.init());
+    S->slots.push_back(std::move(sl));
+  }
+  Server *raw = S.release();
+  raw->worker = std::thread(server_loop, raw);
+  *out = new cyr_server{raw};
+  return CYR_OK;
+}
+
+int cyr_server_submit(cyr_server *s, const cyr_options *opt, const float *optical, const void *voxels,
+                      float *projection, uint32_t device_buffers, uint64_t *id) {
+  if (!s || !id || !optical || !voxels || !projection) return fail(CYR_ERR_ARGUMENT, "null argument");
+  CYR_TRY(validate(opt));
+  auto r = std::make_shared<ServerRequest>();
+  r->opt = *opt;
+  r->energies.assign(opt->energies, opt->energies + opt->num_energies);
+  r->opt.energies = r->energies.data();
+  if (opt->k_vectors && opt->num_k) {
+    r->kvecs.assign(opt->k_vectors, opt->k_vectors + size_t(3) * opt->num_k);
+    r->opt.k_vectors = r->kvecs.data();
+  }
+  r->optical.assign(optical, optical + size_t(opt->num_energies) * opt->num_material * 4);
+  const uint32_t nk = (opt->case_type == 0 && (opt->num_k == 0 || !opt->k_vectors)) ? 1u : opt->num_k;
+  r->vox_bytes = size_t(opt->nx) * opt->ny * opt->nz * opt->num_material * sizeof(float4);
+  r->out_bytes = size_t(opt->num_energies) * nk * opt->nx * opt->ny * sizeof(float);
+  if (device_buffers) {
+    r->d_vox = static_cast<const float4 *>(voxels);
+    r->d_out = projection;
+  } else {
+    r->h_vox = static_cast<const float *>(voxels);
+    r->h_out = projection;
+  }
+  CYR_TRY(plan_request(*r));
+  Server &S = *s->impl;
+  {
+    std::lock_guard<std::mutex> lk(S.mu);
+    r->id = S.next_id++;
+    r->t_submit = Clock::now();
+    S.requests[r->id] = r;
+    S.queue.push_back(r);
+  }
+  S.cv_work.notify_one();
+  *id = r->id;
+  return CYR_OK;
+}
+
+int cyr_server_poll(cyr_server *s, uint64_t id, int *done) {
+  if (!s || !done) return fail(CYR_ERR_ARGUMENT, "null argument");
+  Server &S = *s->impl;
+  std::lock_guard<std::mutex> lk(S.mu);
+  auto it = S.requests.find(id);
+  if (it == S.requests.end()) return fail(CYR_ERR_ARGUMENT, "unknown request id %llu", (unsigned long long)id);
+  *done = it->second->status >= 0 ? 1 : 0;
+  return CYR_OK;
+}
+
+int cyr_server_wait(cyr_server *s, uint64_t id, double *latency_s, double *queue_s) {
+  if (!s) return fail(CYR_ERR_ARGUMENT, "null server");
+  Server &S = *s->impl;
+  std::unique_lock<std::mutex> lk(S.mu);
+  auto it = S.requests.find(id);
+  if (it == S.requests.end()) return fail(CYR_ERR_ARGUMENT, "unknown request id %llu", (unsigned long long)id);
+  std::shared_ptr<ServerRequest> r = it->second;
+  S.cv_done.wait(lk, [&] { return r->status >= 0; });
+  S.requests.erase(it);
+  if (latency_s) *latency_s = std::chrono::duration<double>(r->t_done - r->t_submit).count();
+  if (queue_s) *queue_s = std::chrono::duration<double>(r->t_start - r->t_submit).count();
+  if (r->status != CYR_OK) return fail(r->status, "request %llu: %s", (unsigned long long)id, r->error.c_str());
+  return CYR_OK;
+}
+
+int cyr_server_stats(cyr_server *s, uint64_t *completed, uint64_t *failed, uint64_t *graph_replays,
+                     uint64_t *graph_captures) {
+  if (!s) return fail(CYR_ERR_ARGUMENT, "null server");
+  Server &S = *s->impl;
+  if (completed) *completed = S.completed;
+  if (failed) *failed = S.failed;
+  if (graph_replays) *graph_replays = S.replays;
+  if (graph_captures) *graph_captures = S.captures;
+  return CYR_OK;
+}
+
+int cyr_server_destroy(cyr_server *s) {
+  if (!s) return CYR_OK;
+  const int rc = server_destroy(s->impl);
+  delete s;
+  return rc;
 }
 
 }  // extern "C"

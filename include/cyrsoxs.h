@@ -199,6 +199,49 @@ CYR_API int cyr_profile_end(uint32_t *launches, uint32_t *calls, double *ms, uin
 CYR_API const char *cyr_stage_name(uint32_t stage);
 CYR_API uint32_t cyr_num_stages(void);
 
+
+/* ------------------------------------------------------------------------
+ * Serving: continuous batching of simulation requests on the current device.
+ * No counterpart in the reference, which runs one request per process call.
+ *
+ * A worker thread keeps up to `slots` requests in flight, each on its own
+ * stream with its own scratch, so their work overlaps on the GPU.  Requests
+ * are admitted in submission order as soon as a slot is free and their device
+ * footprint (cyr_required_device_bytes, plus staging for host buffers) fits
+ * in `hbm_budget` bytes next to the requests in flight (0: 85% of the free
+ * memory at creation; a request larger than the budget runs alone).  Each
+ * request computes exactly what cyr_cuda_main computes for it.  With
+ * CYR_SERVER_GRAPHS a slot captures a CUDA graph of a request signature
+ * (options and buffer pointers) the second time it runs it, and replays it
+ * for later requests with the same signature.
+ * ------------------------------------------------------------------------ */
+typedef struct cyr_server cyr_server;
+#define CYR_SERVER_GRAPHS 1u
+
+CYR_API int cyr_server_create(uint32_t slots, size_t hbm_budget, uint32_t flags, cyr_server **server);
+
+/* Queues one request; options, energies, k vectors and optical constants are
+ * copied.  device_buffers = 0: `voxels` [M][Z][Y][X] float4 and `projection`
+ * [E][k][Ny][Nx] are host buffers (pinned memory lets the copies overlap other
+ * requests); 1: device buffers.  They must stay valid until the request is
+ * done.  The AUTO strategy is resolved here. */
+CYR_API int cyr_server_submit(cyr_server *server, const cyr_options *opt, const float *optical, const void *voxels,
+                              float *projection, uint32_t device_buffers, uint64_t *id);
+
+/* done = 1 once the request has finished (its outputs are written). */
+CYR_API int cyr_server_poll(cyr_server *server, uint64_t id, int *done);
+
+/* Blocks until the request has finished and returns its status; latency_s
+ * (submit to completion) and queue_s (submit to admission) may be null.  The
+ * id is forgotten afterwards. */
+CYR_API int cyr_server_wait(cyr_server *server, uint64_t id, double *latency_s, double *queue_s);
+
+CYR_API int cyr_server_stats(cyr_server *server, uint64_t *completed, uint64_t *failed, uint64_t *graph_replays,
+                             uint64_t *graph_captures);
+
+/* Finishes the queued requests, then frees the slots. */
+CYR_API int cyr_server_destroy(cyr_server *server);
+
 #ifdef __cplusplus
 }
 #endif

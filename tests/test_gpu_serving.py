@@ -1,0 +1,127 @@
+"""Serving engine (cyr_server_*): every request gives the same result in the mix
+as alone through cyr_cuda_main, within the parity tolerance, with identical
+NaN masks; admission by footprint, graph capture/replay and device buffers.
+"""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def _setup():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cyrsoxs_gb300 import _native, serving
+
+    return torch, _native, serving
+
+
+def options_for(nat, case, **over):
+    kv = [[0.0, 0.0, 1.0]] if case.case_type == 0 else [cases._normalize32(k).tolist() for k in case.kvecs]
+    kw = dict(nx=case.nx, ny=case.ny, nz=case.nz, num_material=case.num_material, energies=case.energies,
+              start_angle=case.angles[0], end_angle=case.angles[1], increment_angle=case.angles[2],
+              phys_size=case.phys_size, case_type=case.case_type, k_vectors=kv, detector=case.detector,
+              morphology_type=case.morphology, ewald_interpolation=case.interpolation, windowing=case.windowing,
+              scatter_approach=case.scatter, algorithm=case.algorithm, max_streams=case.max_streams,
+              rot_mask=case.rot_mask, reference_frame=case.frame)
+    kw.update(over)
+    return nat.Options(**kw)
+
+
+def same(got, want):
+    assert got.shape == want.shape
+    assert np.array_equal(np.isnan(got), np.isnan(want)), "NaN masks differ"
+    ok = ~np.isnan(want)
+    g, w = got[ok].astype(np.float64), want[ok].astype(np.float64)
+    peak = np.abs(w).max()
+    sel = np.abs(w) > 1e-6 * peak
+    assert (np.abs(g[sel] - w[sel]) / np.abs(w[sel])).max() <= TOL
+
+
+# a mix of shapes, morphologies, frames, interpolation, strategies and sizes
+MIX = ["euler_sphere", "vector_nn_full", "euler_hanning_mask", "material_frame", "beam_divergence", "grazing", "twod",
+       "odd_sizes", "alg1_streams", "four_materials", "nonsquare", "c1_slice"]
+
+
+def mix_requests(nat):
+    reqs = []
+    for i, n in enumerate(MIX):
+        c = cases.CASES[n]
+        strategy = (0, 1, 2)[i % 3]
+        reqs.append((n, options_for(nat, c, strategy=strategy), cases.optical_constants(c),
+                     np.ascontiguousarray(cases.voxels(c), np.float32), c))
+    return reqs
+
+
+def out_for(nat, opts, c):
+    s = opts.struct
+    return np.zeros((s.num_energies, opts.num_k, s.ny, s.nx), np.float32)
+
+
+def test_each_request_is_the_same_alone_and_in_the_mix():
+    torch, nat, serving = _setup()
+    reqs = mix_requests(nat)
+    alone = {n: nat.cuda_main(o, opt, v, streams_variant=c.algorithm == 1) for n, o, opt, v, c in reqs}
+    with serving.Server(slots=4, graphs=True) as srv:
+        for rnd in range(3):  # repeats: warm runs, graph captures, replays
+            outs, ids = {}, {}
+            for n, o, opt, v, c in reqs:
+                outs[n] = out_for(nat, o, c)
+                ids[n] = srv.submit(o, opt, v, outs[n])
+            for n in ids:
+                lat, q = srv.wait(ids[n])
+                assert lat >= q >= 0.0
+                same(outs[n], alone[n])
+        st = srv.stats()
+    assert st["completed"] == 3 * len(reqs) and st["failed"] == 0
+
+
+def test_one_slot_captures_then_replays_a_repeated_signature():
+    torch, nat, serving = _setup()
+    n, o, opt, v, c = mix_requests(nat)[1]
+    want = nat.cuda_main(o, opt, v)
+    with serving.Server(slots=1, graphs=True) as srv:
+        for _ in range(4):
+            out = out_for(nat, o, c)
+            srv.wait(srv.submit(o, opt, v, out))
+            same(out, want)
+        st = srv.stats()
+    assert st["graph_captures"] == 1 and st["graph_replays"] == 2
+
+
+def test_budget_smaller_than_a_request_still_runs_requests_one_at_a_time():
+    torch, nat, serving = _setup()
+    reqs = mix_requests(nat)[:4]
+    with serving.Server(slots=4, hbm_budget=1) as srv:
+        outs = [out_for(nat, o, c) for _, o, _, _, c in reqs]
+        ids = [srv.submit(o, opt, v, out) for (_, o, opt, v, _), out in zip(reqs, outs)]
+        for (n, o, opt, v, c), out, rid in zip(reqs, outs, ids):
+            srv.wait(rid)
+            same(out, nat.cuda_main(o, opt, v, streams_variant=c.algorithm == 1))
+
+
+def test_device_buffers():
+    torch, nat, serving = _setup()
+    n, o, opt, v, c = mix_requests(nat)[0]
+    want = nat.cuda_main(o, opt, v)
+    dv = torch.from_numpy(v).cuda()
+    dout = torch.zeros(want.size, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    with serving.Server(slots=2) as srv:
+        srv.wait(srv.submit(o, opt, dv.data_ptr(), dout.data_ptr(), device=True))
+    same(dout.cpu().numpy().reshape(want.shape), want)
+
+
+def test_invalid_request_is_rejected_at_submit():
+    torch, nat, serving = _setup()
+    bad = nat.Options(nx=22, ny=8, nz=4, num_material=1, energies=[285.0], start_angle=0, end_angle=0,
+                      increment_angle=0, phys_size=5.0)
+    with serving.Server(slots=1) as srv:
+        with pytest.raises(nat.CyrError):
+            srv.submit(bad, np.zeros((1, 1, 4), np.float32), np.zeros((1, 4, 8, 22, 4), np.float32),
+                       np.zeros((1, 1, 8, 22), np.float32))
