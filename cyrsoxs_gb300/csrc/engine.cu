@@ -965,7 +965,6 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
       CYR_CUDA(cudaGetLastError());
     }
   }
-  CYR_CUDA(cudaEventRecord(sc.last_use, st));
   return CYR_OK;
 }
 
@@ -977,15 +976,17 @@ struct RunMode {
   unsigned char *host_arena = nullptr;
   size_t host_arena_bytes = 0;
   bool capturing = false;
+  const Plan *plan = nullptr;  // made by the caller for these options (strategy resolved), or null
 };
 
 int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const float *optical, const float4 *d_vox,
                 float *d_out, cudaStream_t st, const RunMode &mode = RunMode()) {
-  Plan pl;
-  CYR_TRY(make_plan(o, optical, pl));
+  Plan local;
+  if (!mode.plan) CYR_TRY(make_plan(o, optical, local));
+  Plan &pl = mode.plan ? const_cast<Plan &>(*mode.plan) : local;
   CYR_TRY(setup_attrs(ctx));
   CYR_TRY(sc.init());
-  if (pl.fields && o->strategy == CYR_STRATEGY_AUTO && !mode.capturing) {
+  if (!mode.plan && pl.fields && o->strategy == CYR_STRATEGY_AUTO && !mode.capturing) {
     // AUTO falls back to the per-energy spectra when the field volumes do not fit
     size_t free_b = 0, total_b = 0;
     CYR_CUDA(cudaMemGetInfo(&free_b, &total_b));
@@ -1045,7 +1046,12 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
       k_moments<1><<<grid, 256, 0, st>>>(mp);
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
-    if (pl.fields) return run_fields(ctx, sc, o, pl, dp, d_vox, d_out, st);
+    if (pl.fields) {
+      CYR_TRY(run_fields(ctx, sc, o, pl, dp, d_vox, d_out, st));
+      // an event recorded inside a capture cannot be waited on outside it (slots keep order by their stream)
+      if (!mode.capturing) CYR_CUDA(cudaEventRecord(sc.last_use, st));
+      return CYR_OK;
+    }
     slot = ctx.prof.begin(kMeans, st);
     k_entry_means<<<1, 64, 0, st>>>(sc.moments.as<double>(), pl.nmat, pl.nvox,
                                     reinterpret_cast<const MaterialConsts *>(dp + pl.off_mc), pl.ne,
@@ -1294,7 +1300,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
       CYR_CUDA(cudaGetLastError());
     }
   }
-  CYR_CUDA(cudaEventRecord(sc.last_use, st));
+  if (!mode.capturing) CYR_CUDA(cudaEventRecord(sc.last_use, st));
   return CYR_OK;
 }
 
@@ -1324,6 +1330,8 @@ struct ServerRequest {
   float *d_out = nullptr;
   size_t vox_bytes = 0, out_bytes = 0, footprint = 0;
   std::string key;  // graph signature
+  Plan plan;        // host plan (strategy resolved), made once at submit
+  double work = 0;  // share of the GPU the request fills (1 = saturating)
   int status = -1;  // -1 queued or running, else a CYR_* code
   std::string error;
   Clock::time_point t_submit, t_start, t_done;
@@ -1353,6 +1361,7 @@ struct Server {
   int device = 0;
   std::vector<std::unique_ptr<Slot>> slots;
   size_t budget = 0, in_use = 0;
+  double inflight_work = 0;
   bool graphs = false;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -1366,19 +1375,27 @@ struct Server {
 
 // Host planning for one request: resolve the AUTO strategy (so a signature
 // always means the same launch sequence) and compute its footprint.
-int plan_request(ServerRequest &r) {
-  Plan pl;
+// Voxel-materials one request needs to fill the GPU on its own; smaller
+// requests leave room for others to run beside them.
+constexpr double kSaturatingWork = 8.0e6;
+// Requests in flight at once, in units of GPU-filling requests: beyond about
+// two, concurrency only time-slices large requests and lengthens latency.
+constexpr double kMaxInflightWork = 2.0;
+
+int plan_request(ServerRequest &r, bool staged) {
+  Plan &pl = r.plan;
   CYR_TRY(make_plan(&r.opt, r.optical.data(), pl));
   if (r.opt.strategy == CYR_STRATEGY_AUTO) r.opt.strategy = pl.fields ? CYR_STRATEGY_FIELDS : CYR_STRATEGY_PER_ENERGY;
-  r.footprint = request_bytes(pl) + (r.h_vox ? r.vox_bytes + r.out_bytes : 0);
+  r.footprint = request_bytes(pl) + (staged ? r.vox_bytes + r.out_bytes : 0);
+  r.work = std::min(1.0, double(pl.nvox) * pl.nmat / kSaturatingWork);
   char head[256];
   std::snprintf(head, sizeof head, "%u,%u,%u,%u,%u,%a,%a,%a,%a,%u,%u,%u,%u,%u,%u,%u,%u,%u,%u,%u,%a,%a,%a|%p|%p|",
                 r.opt.nx, r.opt.ny, r.opt.nz, r.opt.num_material, r.opt.num_energies, double(r.opt.start_angle),
                 double(r.opt.end_angle), double(r.opt.increment_angle), double(r.opt.phys_size), r.opt.case_type,
                 r.opt.num_k, r.opt.morphology_type, r.opt.ewald_interpolation, r.opt.windowing,
                 r.opt.scatter_approach, r.opt.algorithm, r.opt.rot_mask, r.opt.reference_frame, r.opt.strategy,
-                r.h_vox ? 1u : 0u, double(r.opt.detector[0]), double(r.opt.detector[1]), double(r.opt.detector[2]),
-                static_cast<const void *>(r.d_vox), static_cast<void *>(r.d_out));
+                staged ? 1u : 0u, double(r.opt.detector[0]), double(r.opt.detector[1]), double(r.opt.detector[2]),
+                staged ? nullptr : static_cast<const void *>(r.d_vox), staged ? nullptr : static_cast<void *>(r.d_out));
   r.key = head;
   for (float e : r.energies) r.key += std::to_string(e) + ",";
   for (float k : r.kvecs) r.key += std::to_string(k) + ",";
@@ -1386,19 +1403,25 @@ int plan_request(ServerRequest &r) {
 }
 
 // Enqueues request r on slot sl (worker thread).
+// Host buffers always go through the slot's staging buffers; with graphs,
+// device buffers do too (device-to-device), so a signature does not depend on
+// the caller's pointers and one graph serves every morphology of a shape.
+bool staged_request(const Server &S, const ServerRequest &r) { return r.h_vox != nullptr || S.graphs; }
+
 int start_request(Server &S, Slot &sl, ServerRequest &r) {
   cudaStream_t st = sl.stream;
   const float4 *d_vox = r.d_vox;
   float *d_out = r.d_out;
-  if (r.h_vox) {
+  const bool staged = staged_request(S, r);
+  if (staged) {
     CYR_TRY(sl.vox.ensure(r.vox_bytes));
     CYR_TRY(sl.out.ensure(r.out_bytes));
-    CYR_CUDA(cudaMemcpyAsync(sl.vox.ptr, r.h_vox, r.vox_bytes, cudaMemcpyHostToDevice, st));
+    CYR_CUDA(cudaMemcpyAsync(sl.vox.ptr, r.h_vox ? static_cast<const void *>(r.h_vox) : r.d_vox, r.vox_bytes,
+                             r.h_vox ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
     d_vox = sl.vox.as<float4>();
     d_out = sl.out.as<float>();
   }
-  Plan pl;
-  CYR_TRY(make_plan(&r.opt, r.optical.data(), pl));
+  const Plan &pl = r.plan;
   if (pl.arena.size() > sl.host_arena_bytes) {
     if (sl.host_arena) {
       CYR_CUDA(cudaStreamSynchronize(st));
@@ -1413,6 +1436,7 @@ int start_request(Server &S, Slot &sl, ServerRequest &r) {
   RunMode mode;
   mode.host_arena = sl.host_arena;
   mode.host_arena_bytes = sl.host_arena_bytes;
+  mode.plan = &r.plan;
   auto git = S.graphs ? sl.graphs.find(r.key) : sl.graphs.end();
   if (git != sl.graphs.end() && git->second.generation == sl.generation()) {
     std::memcpy(sl.host_arena, pl.arena.data(), pl.arena.size());
@@ -1450,7 +1474,9 @@ int start_request(Server &S, Slot &sl, ServerRequest &r) {
     }
   }
   CYR_CUDA(cudaMemcpyAsync(sl.host_errors, sl.sc.errors.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-  if (r.h_out) CYR_CUDA(cudaMemcpyAsync(r.h_out, d_out, r.out_bytes, cudaMemcpyDeviceToHost, st));
+  if (staged)
+    CYR_CUDA(cudaMemcpyAsync(r.h_out ? static_cast<void *>(r.h_out) : static_cast<void *>(r.d_out), d_out, r.out_bytes,
+                             r.h_out ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
   CYR_CUDA(cudaEventRecord(sl.done, st));
   return CYR_OK;
 }
@@ -1463,6 +1489,7 @@ void finish_request(Server &S, Slot &sl, int status, const std::string &err) {
   r->status = status;
   r->error = err;
   S.in_use -= std::min(S.in_use, r->footprint);
+  S.inflight_work = std::max(0.0, S.inflight_work - r->work);
   if (status == CYR_OK)
     ++S.completed;
   else
@@ -1498,19 +1525,34 @@ void server_loop(Server *Sp) {
       std::shared_ptr<ServerRequest> r;
       Slot *free_slot = nullptr;
       bool any_active = false;
+      {
+        std::lock_guard<std::mutex> lk(S.mu);
+        if (S.queue.empty()) break;
+        r = S.queue.front();
+      }
+      // a free slot, preferring one that holds this signature's graph or warm state
+      int best = -1;
       for (auto &slp : S.slots) {
-        if (slp->req)
+        Slot &sl = *slp;
+        if (sl.req) {
           any_active = true;
-        else if (!free_slot)
-          free_slot = slp.get();
+          continue;
+        }
+        auto g = sl.graphs.find(r->key);
+        auto wm = sl.warm.find(r->key);
+        const int score = (g != sl.graphs.end() && g->second.generation == sl.generation())  ? 2
+                          : (wm != sl.warm.end() && wm->second == sl.generation()) ? 1
+                                                                                    : 0;
+        if (score > best) best = score, free_slot = &sl;
       }
       {
         std::lock_guard<std::mutex> lk(S.mu);
-        if (S.queue.empty() || !free_slot) break;
-        r = S.queue.front();
-        if (any_active && S.in_use + r->footprint > S.budget) break;
+        if (!free_slot) break;
+        if (any_active && (S.in_use + r->footprint > S.budget || S.inflight_work + r->work > kMaxInflightWork))
+          break;
         S.queue.pop_front();
         S.in_use += r->footprint;
+        S.inflight_work += r->work;
         r->t_start = Clock::now();
       }
       progress = true;
@@ -1918,8 +1960,8 @@ int cyr_server_submit(cyr_server *s, const cyr_options *opt, const float *optica
     r->h_vox = static_cast<const float *>(voxels);
     r->h_out = projection;
   }
-  CYR_TRY(plan_request(*r));
   Server &S = *s->impl;
+  CYR_TRY(plan_request(*r, staged_request(S, *r)));
   {
     std::lock_guard<std::mutex> lk(S.mu);
     r->id = S.next_id++;

@@ -125,3 +125,20 @@ def test_invalid_request_is_rejected_at_submit():
         with pytest.raises(nat.CyrError):
             srv.submit(bad, np.zeros((1, 1, 4), np.float32), np.zeros((1, 4, 8, 22, 4), np.float32),
                        np.zeros((1, 1, 8, 22), np.float32))
+
+
+def test_one_slot_alternating_signatures_after_a_capture():
+    # A runs warm, is captured, then B runs uncaptured on the same slot after A's graph, and so on
+    torch, nat, serving = _setup()
+    reqs = mix_requests(nat)
+    a, b = reqs[1], reqs[2]
+    want = {r[0]: nat.cuda_main(r[1], r[2], r[3]) for r in (a, b)}
+    with serving.Server(slots=1, graphs=True) as srv:
+        for r in (a, a, b, a, b, b, a):
+            n, o, opt, v, c = r
+            out = out_for(nat, o, c)
+            srv.wait(srv.submit(o, opt, v, out))
+            same(out, want[n])
+        st = srv.stats()
+    # B's first run may grow the slot's buffers, which retires A's graph (it is captured again later)
+    assert st["failed"] == 0 and st["graph_captures"] >= 2 and st["graph_replays"] >= 1
