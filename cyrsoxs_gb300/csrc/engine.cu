@@ -20,7 +20,7 @@
 // morphology fields are formed once per request; every energy and angle is
 // combined from them inside the Ewald kernel, batched over energies:
 //
-//   k_moments -> k_field_means -> k_build_fields -> 3D FFT -> k_dc -> per k and
+//   k_moments -> k_build_fields -> 3D FFT -> per k and
 //   energy batch: k_ewald_fields -> k_rotate_average -> k_fill + k_warp
 //
 // All per-request constants (optical constants of every energy, angle
@@ -365,6 +365,33 @@ int warp_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, ui
   return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st);
 }
 
+// One y or z pass with k_fft_thread (lines of 8..64, one thread per line).
+int thread_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
+                    cudaStream_t st) {
+  const uint32_t n = axis == 1 ? ny : nz;
+  const float2 *tw = nullptr;
+  CYR_TRY(get_twiddles(ctx, n, &tw));
+  ThreadPassParams p{};
+  p.data = data;
+  p.nx = nx;
+  p.vstride = size_t(nx) * ny * nz;
+  p.tw = tw;
+  if (axis == 1) {
+    p.others = nz, p.ostride = size_t(nx) * ny, p.estride = nx;
+  } else {
+    p.others = ny, p.ostride = nx, p.estride = size_t(nx) * ny;
+  }
+  const dim3 grid(unsigned((size_t(nx) * p.others + 127) / 128), count);
+  const int slot = ctx.prof.begin(axis == 1 ? kFftColsY : kFftColsZ, st);
+  if (n == 8) k_fft_thread<8><<<grid, 128, 0, st>>>(p);
+  if (n == 16) k_fft_thread<16><<<grid, 128, 0, st>>>(p);
+  if (n == 32) k_fft_thread<32><<<grid, 128, 0, st>>>(p);
+  if (n == 64) k_fft_thread<64><<<grid, 128, 0, st>>>(p);
+  ctx.prof.end(slot, st);
+  CYR_CUDA(cudaGetLastError());
+  return CYR_OK;
+}
+
 // In-place forward 3D FFT of `count` volumes.
 int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
           bool skip_z = false) {
@@ -375,6 +402,10 @@ int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t n
     if (n == 1) continue;
     if (n == 128 || n == 256 || n == 512) {
       CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st));
+      continue;
+    }
+    if (axis > 0 && (n == 8 || n == 16 || n == 32 || n == 64) && count <= 65535) {
+      CYR_TRY(thread_fft_pass(ctx, data, nx, ny, nz, count, axis, st));
       continue;
     }
     FftPassParams p{};
@@ -844,23 +875,17 @@ EwaldParams ewald_params(const Plan &pl, const cyr_options *o, const unsigned ch
 // every energy (in batches) and k from them.
 int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan &pl, const unsigned char *dp,
                const float4 *d_vox, float *d_out, cudaStream_t st) {
-  const uint32_t nf = num_fields(pl.nmat), npk = pl.npk;
-  CYR_TRY(sc.fmean.ensure(nf * sizeof(float)));
+  const uint32_t npk = pl.npk;
   CYR_TRY(sc.spec.ensure(size_t(npk) * pl.nvox * sizeof(float2)));
-  CYR_TRY(sc.dc.ensure(size_t(npk) * sizeof(float2)));
   CYR_TRY(sc.images.ensure(size_t(pl.ebatch) * image_bytes(pl)));
   CYR_TRY(sc.avg.ensure(size_t(pl.ebatch) * pl.npix * sizeof(float)));
   float2 *spec = sc.spec.as<float2>();
-  int slot = ctx.prof.begin(kFieldMeans, st);
-  k_field_means<<<1, 128, 0, st>>>(sc.moments.as<double>(), pl.nmat,
-                                   pl.npix * ((pl.nz + pl.mom_zstep - 1) / pl.mom_zstep), sc.fmean.as<float>());
-  ctx.prof.end(slot, st);
-  CYR_CUDA(cudaGetLastError());
   FieldParams fp{};
   fp.vox = d_vox;
   fp.nx = pl.nx, fp.ny = pl.ny, fp.nz = pl.nz, fp.nmat = pl.nmat;
   fp.nvox = pl.nvox;
-  fp.mean = sc.fmean.as<float>();
+  fp.mom = sc.moments.as<double>();  // each block forms the field means from the moments
+  fp.nsamp = pl.npix * ((pl.nz + pl.mom_zstep - 1) / pl.mom_zstep);
   if (pl.hanning) {
     fp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
     fp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
@@ -870,7 +895,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   int sms = 0;
   CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
   const uint32_t blocks = uint32_t(std::min<size_t>((pl.nvox + 255) / 256, size_t(sms) * 8));
-  slot = ctx.prof.begin(kBuildFields, st);
+  int slot = ctx.prof.begin(kBuildFields, st);
   if (o->morphology_type == 0)
     k_build_fields<0><<<blocks, 256, 0, st>>>(fp);
   else
@@ -878,15 +903,9 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   ctx.prof.end(slot, st);
   CYR_CUDA(cudaGetLastError());
   CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st));
-  slot = ctx.prof.begin(kDc, st);
-  k_dc<<<1, (npk + 31) / 32 * 32, 0, st>>>(spec, npk, pl.nvox, pl.nx, pl.ny, pl.nz, 0, 1 % pl.nz, pl.nz - 1,
-                                           sc.dc.as<float2>());
-  ctx.prof.end(slot, st);
-  CYR_CUDA(cudaGetLastError());
 
   FieldEwaldParams fe{};
-  fe.zspec = spec;
-  fe.zdc = sc.dc.as<float2>();
+  fe.zspec = spec;  // every Ewald block forms the DC replacement of each packed volume
   fe.npk = npk;
   fe.nvox = pl.nvox;
   fe.coef = reinterpret_cast<const float4 *>(dp + pl.off_fcoef);
@@ -1038,7 +1057,10 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
     mp.neg = sc.flags.as<unsigned>();
     int nsm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx.device));
-    const dim3 grid(uint32_t(std::max<size_t>(1, std::min<size_t>((pl.nvox + 255) / 256, size_t(nsm) * 8))), pl.nmat);
+    // about 8 samples per thread: small volumes get few blocks (each block ends in
+    // kMoments double atomics on the same addresses), large ones 4 per SM
+    const size_t nsamp = pl.npix * ((pl.nz + mp.zstep - 1) / mp.zstep);
+    const dim3 grid(uint32_t(std::max<size_t>(1, std::min<size_t>((nsamp + 2047) / 2048, size_t(nsm) * 4))), pl.nmat);
     int slot = ctx.prof.begin(kMom, st);
     if (o->morphology_type == 0)
       k_moments<0><<<grid, 256, 0, st>>>(mp);

@@ -32,12 +32,16 @@ constexpr int kFieldsPerMaterial = 7;
 __host__ __device__ constexpr uint32_t num_fields(uint32_t nmat) { return kFieldsPerMaterial * nmat + 1; }
 __host__ __device__ constexpr uint32_t num_packed(uint32_t nmat) { return (num_fields(nmat) + 1) / 2; }
 
+constexpr uint32_t kMaxFields = num_fields(kMaxMaterials);
+constexpr uint32_t kMaxPacked = num_packed(kMaxMaterials);
+
 // Field means from the per-material moments (k_moments over nsamp voxels), T
-// last.  Any constant subtracted from a field changes only bin 0, which is
-// replaced, so the means need only be close (a z-plane subsample suffices);
-// they keep the FP32 rounding of the transform proportional to the
-// fluctuations.
-__global__ void k_field_means(const double *__restrict__ mom, uint32_t nmat, size_t nsamp, float *__restrict__ out) {
+// last, computed by the calling block.  Any constant subtracted from a field
+// changes only bin 0, which is replaced, so the means need only be close (a
+// z-plane subsample suffices); they keep the FP32 rounding of the transform
+// proportional to the fluctuations.
+__device__ __forceinline__ void field_means(const double *__restrict__ mom, uint32_t nmat, size_t nsamp,
+                                            float *__restrict__ out) {
   const uint32_t nf = num_fields(nmat);
   for (uint32_t g = threadIdx.x; g < nf; g += blockDim.x) {
     double v = 0.0;
@@ -57,7 +61,8 @@ struct FieldParams {
   const float4 *vox;     // [nmat][nvox] as the reference stores Voxel::s1
   uint32_t nx, ny, nz, nmat;
   size_t nvox;
-  const float *mean;     // [num_fields] volume mean of each windowed field
+  const double *mom;     // [nmat][kMoments] moment sums over nsamp voxels
+  size_t nsamp;
   const float *hann_x, *hann_y, *hann_z;  // null when no windowing
   float2 *out;           // [num_packed][nvox]: field 2j in .x, field 2j+1 in .y
 };
@@ -65,6 +70,9 @@ struct FieldParams {
 // Windowed, mean-free fields of every voxel, packed in pairs.
 template <int MORPH>
 __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
+  __shared__ float mean[kMaxFields];  // volume mean of each windowed field
+  field_means(p.mom, p.nmat, p.nsamp, mean);
+  __syncthreads();
   const size_t stride = size_t(gridDim.x) * blockDim.x;
   for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
     float w = 1.f;
@@ -77,7 +85,7 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
     float2 *o = p.out + i;
     // g is the same in every thread: the parity branches do not diverge
     auto emit = [&](float v) {
-      v -= p.mean[g];
+      v -= mean[g];
       if (g & 1u)
         o[size_t(g >> 1) * p.nvox] = make_float2(pend, v);
       else
@@ -112,7 +120,7 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
 // rotation R^T folded in, include/uniaxial.h:163-165).
 struct FieldEwaldParams {
   const float2 *zspec;   // [npk][nz][ny][nx], unshifted (natural) bin order
-  const float2 *zdc;     // [npk] DC replacement of each packed volume
+  // the DC replacement of each packed volume is formed by every block (dc_mean)
   uint32_t npk;
   size_t nvox;
   const float4 *coef;    // [ne][6][npk]: (alpha.x, alpha.y, beta.x, beta.y)
@@ -140,10 +148,13 @@ constexpr int kFieldGather = 4;  // packed volumes whose loads are issued togeth
 template <int NB>
 __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldParams p) {
   extern __shared__ float4 fcoef[];  // [6][npk]
+  __shared__ float2 zdc[kMaxPacked];
   const uint32_t eb = blockIdx.x % p.nbatch, e = p.e0 + eb;
-  for (uint32_t t = threadIdx.x; t < 6 * p.npk; t += blockDim.x) fcoef[t] = p.coef[size_t(e) * 6 * p.npk + t];
-  __syncthreads();
   const uint32_t nx = p.g.nx, ny = p.g.ny, nz = p.g.nz;
+  for (uint32_t t = threadIdx.x; t < 6 * p.npk; t += blockDim.x) fcoef[t] = p.coef[size_t(e) * 6 * p.npk + t];
+  for (uint32_t j = threadIdx.x; j < p.npk; j += blockDim.x)
+    zdc[j] = dc_mean(p.zspec + size_t(j) * p.nvox, nx, ny, nz, 0, 1 % nz, nz - 1);
+  __syncthreads();
   const size_t npix = size_t(nx) * ny;
   const size_t t = size_t(blockIdx.x / p.nbatch) * blockDim.x + threadIdx.x;
   if (t >= npix) return;
@@ -190,7 +201,7 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
         za[q] = zb[q] = make_float2(0.f, 0.f);
         if (j < p.npk) {
           if (is_dc) {
-            za[q] = zb[q] = p.zdc[j];
+            za[q] = zb[q] = zdc[j];
           } else {
             const float2 *zj = p.zspec + size_t(j) * p.nvox;
             za[q] = __ldg(&zj[i0]);

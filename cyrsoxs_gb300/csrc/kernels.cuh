@@ -740,7 +740,63 @@ __global__ void __launch_bounds__(TX * 32) k_fft_cols(ColPassParams p) {
   }
 }
 
-// Warp-FFT form of k_build_fft_z// Tensor build fused with the z-axis FFT, keeping only the z planes the Ewald
+// Warp-FFT form of k_build_fft_z// Per-thread register FFT for short strided lines (N = 8..64, powers of two):
+// one thread owns one y or z line, and consecutive threads take consecutive
+// x, so each of a warp's N loads and N stores is one contiguous 256-byte
+// segment and no shared memory is involved.  Radix-2 decimation in
+// frequency, fully unrolled (every index is a compile-time constant); the
+// result is read out in bit-reversed order.
+__host__ __device__ constexpr int bitrev(int k, int bits) {
+  int r = 0;
+  for (int b = 0; b < bits; ++b)
+    if ((k >> b) & 1) r |= 1 << (bits - 1 - b);
+  return r;
+}
+
+template <int N>
+__device__ __forceinline__ void fft_reg(float2 (&a)[N], const float2 *__restrict__ tw) {
+#pragma unroll
+  for (int len = N; len >= 2; len >>= 1) {
+    const int half = len >> 1, step = N / len;
+#pragma unroll
+    for (int start = 0; start < N; start += len)
+#pragma unroll
+      for (int j = 0; j < half; ++j) {
+        const float2 u = a[start + j], v = a[start + j + half];
+        a[start + j] = cadd(u, v);
+        const float2 d = csub(u, v);
+        a[start + j + half] = j == 0 ? d : cmul(d, __ldg(&tw[j * step]));
+      }
+  }
+}
+
+struct ThreadPassParams {
+  float2 *data;
+  uint32_t nx;       // lines per row of lines (x)
+  uint32_t others;   // rows of lines: ny (z pass) or nz (y pass)
+  size_t ostride;    // elements between rows of lines: nx (z pass) or nx * ny (y pass)
+  size_t estride;    // elements between the points of a line: nx * ny (z) or nx (y)
+  size_t vstride;    // elements between volumes (blockIdx.y)
+  const float2 *tw;  // W_N^m, m < N
+};
+
+template <int N>
+__global__ void __launch_bounds__(128) k_fft_thread(ThreadPassParams p) {
+  constexpr int BITS = N == 8 ? 3 : N == 16 ? 4 : N == 32 ? 5 : 6;
+  const size_t lines = size_t(p.nx) * p.others;
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= lines) return;
+  const uint32_t x = uint32_t(t % p.nx);
+  float2 *g = p.data + size_t(blockIdx.y) * p.vstride + (t / p.nx) * p.ostride + x;
+  float2 a[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) a[i] = g[i * p.estride];
+  fft_reg<N>(a, p.tw);
+#pragma unroll
+  for (int k = 0; k < N; ++k) g[k * p.estride] = a[bitrev(k, BITS)];
+}
+
+// Tensor build fused with the z-axis FFT, keeping only the z planes the Ewald
 // projection can read.  A block owns TX consecutive x columns at one y, over
 // all z: it computes the nvol entry volumes for those columns into shared
 // memory, transforms them along z, and writes planes [zlo, zlo + kz) of the
@@ -886,12 +942,11 @@ __global__ void __launch_bounds__(256) k_build_fft_z_warp(BuildZParams p, const 
 // The spectra are stored as planes: plane pz of volume v starts at
 // spec + v * vstride + pz * nx * ny.  p0, p1, pn are the planes holding the
 // unshifted z bins 0, 1 and nz-1.
-__global__ void k_dc(const float2 *__restrict__ spec, uint32_t nvol, size_t vstride, uint32_t nx, uint32_t ny,
-                     uint32_t nz, uint32_t p0, uint32_t p1, uint32_t pn, float2 *__restrict__ dc) {
-  const uint32_t v = threadIdx.x;
-  if (v >= nvol) return;
+// Mean of the DC bin's neighbours (4 in 2D, else 6) of one volume whose z
+// planes of unshifted bins 0, 1 and nz-1 are p0, p1 and pn.
+__device__ __forceinline__ float2 dc_mean(const float2 *__restrict__ V, uint32_t nx, uint32_t ny, uint32_t nz,
+                                          uint32_t p0, uint32_t p1, uint32_t pn) {
   const size_t P = size_t(nx) * ny;
-  const float2 *V = spec + size_t(v) * vstride;
   const float2 *Z0 = V + size_t(p0) * P;
   float2 s = make_float2(0.f, 0.f);
   s = cadd(s, Z0[1]);
@@ -904,7 +959,14 @@ __global__ void k_dc(const float2 *__restrict__ spec, uint32_t nvol, size_t vstr
     s = cadd(s, V[size_t(pn) * P]);
     cnt = 6.f;
   }
-  dc[v] = make_float2(s.x / cnt, s.y / cnt);
+  return make_float2(s.x / cnt, s.y / cnt);
+}
+
+__global__ void k_dc(const float2 *__restrict__ spec, uint32_t nvol, size_t vstride, uint32_t nx, uint32_t ny,
+                     uint32_t nz, uint32_t p0, uint32_t p1, uint32_t pn, float2 *__restrict__ dc) {
+  const uint32_t v = threadIdx.x;
+  if (v >= nvol) return;
+  dc[v] = dc_mean(spec + size_t(v) * vstride, nx, ny, nz, p0, p1, pn);
 }
 
 // ---------------------------------------------------------------------------
