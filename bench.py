@@ -61,6 +61,10 @@ def parse():
                     help="0 auto, 1 per-energy spectra, 2 field spectra once per request")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-served", action="store_true", help="skip the batched and serving measurements")
+    ap.add_argument("--served-only", action="store_true", help="only the batched and serving measurements")
+    ap.add_argument("--slots", type=int, default=8, help="serving slots (requests in flight)")
+    ap.add_argument("--serve-requests", type=int, default=80)
     return ap.parse_args()
 
 
@@ -251,6 +255,149 @@ def run_reference(args):
     return 0
 
 
+def _pct(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, max(0, int(math.ceil(q * len(xs))) - 1))]
+
+
+def _lat_summary(lat_s):
+    return {"p50_ms": 1000 * _pct(lat_s, 0.50), "p99_ms": 1000 * _pct(lat_s, 0.99), "max_ms": 1000 * max(lat_s)}
+
+
+def served_benchmarks(args):
+    """Batched and served throughput against the plain one-request-at-a-time
+    path on the same GPU, with p50/p99 request latency.
+
+    batched: the 64 uneven two-phase morphologies (20 energies x 12 E angles),
+    all submitted at t = 0, device-resident (plain = cyr_simulate_device and a
+    synchronisation per request, in order) and again from pinned host memory
+    (plain = cyr_cuda_main per request); served = the serving engine
+    (continuous batching over `--slots` slots, CUDA graphs).
+    serving: a seeded Poisson stream (200 requests/s) of requests of random
+    size, materials, energies and angles with device-resident morphologies;
+    plain = the same arrivals served one at a time in arrival order.  Each
+    mode runs once untimed first (scratch, autotuning, graph capture)."""
+    import torch
+
+    from cyrsoxs_gb300 import _native, serving, workloads
+
+    def opts_for(w, strategy=0):
+        return _native.Options(nx=w.nx, ny=w.ny, nz=w.nz, num_material=w.num_material, energies=w.energies,
+                               start_angle=w.angles[0], end_angle=w.angles[1], increment_angle=w.angles[2],
+                               phys_size=w.phys_size, morphology_type=0, strategy=strategy)
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+
+    out = {}
+    cs = torch.cuda.current_stream()
+    # ---- batched: 64 uneven morphologies ----
+    reqs = []
+    for w in workloads.batched_set():
+        dv = workloads.voxels_torch(w).contiguous()
+        hv = pinned((w.num_material, w.nz, w.ny, w.nx, 4))
+        hv[...] = dv.cpu().numpy()
+        reqs.append((opts_for(w), workloads.optical_constants(w), dv,
+                     torch.empty(len(w.energies) * w.ny * w.nx, dtype=torch.float32, device="cuda"), hv,
+                     pinned((len(w.energies), 1, w.ny, w.nx)), len(w.energies) * w.num_angles()))
+    torch.cuda.synchronize()
+    patterns = sum(r[6] for r in reqs)
+
+    def plain_batch(host):
+        t0 = time.perf_counter()
+        lat = []
+        for o, opt, dv, dout, hv, hout, _ in reqs:
+            if host:
+                _native.cuda_main(o, opt, hv, out=hout)
+            else:
+                _native.simulate_device(o, opt, dv.data_ptr(), dout.data_ptr(), cs.cuda_stream)
+                cs.synchronize()
+            lat.append(time.perf_counter() - t0)
+        return time.perf_counter() - t0, lat
+
+    def served_batch(srv, host):
+        t0 = time.perf_counter()
+        if host:
+            ids = [srv.submit(o, opt, hv, hout) for o, opt, dv, dout, hv, hout, _ in reqs]
+        else:
+            ids = [srv.submit(o, opt, dv.data_ptr(), dout.data_ptr(), device=True)
+                   for o, opt, dv, dout, hv, hout, _ in reqs]
+        lat = [srv.wait(i)[0] for i in ids]
+        return time.perf_counter() - t0, lat
+
+    for host, name, where in ((False, "batched", "device-resident morphologies and patterns"),
+                              (True, "batched_host_buffers", "morphologies and patterns in pinned host memory "
+                                                            "(host<->device copies inside the timed region)")):
+        plain_batch(host)
+        tp, lp = plain_batch(host)
+        with serving.Server(slots=args.slots, graphs=True) as srv:
+            served_batch(srv, host)
+            ts, ls = served_batch(srv, host)
+            st = srv.stats()
+        out[name] = {
+            "config": "64 seeded two-phase Euler morphologies, X = Y in {64,128,256}, Z in {16,32,64}; 20 energies x "
+                      f"12 E angles each; {where}; all requests at t = 0",
+            "requests": len(reqs), "patterns": patterns,
+            "plain": {"patterns_per_s": patterns / tp, "seconds": tp, **_lat_summary(lp)},
+            "served": {"patterns_per_s": patterns / ts, "seconds": ts, "slots": args.slots, "graphs": True,
+                       "graph_replays": st["graph_replays"], "graph_captures": st["graph_captures"],
+                       **_lat_summary(ls)},
+            "speedup": tp / ts,
+        }
+    del reqs
+    # ---- serving: Poisson stream, device-resident morphologies ----
+    stream_reqs = []
+    for arrival, w in workloads.serving_stream(args.serve_requests):
+        dv = workloads.voxels_torch(w).contiguous()
+        dout = torch.empty(len(w.energies) * w.ny * w.nx, dtype=torch.float32, device="cuda")
+        stream_reqs.append((arrival, opts_for(w), workloads.optical_constants(w), dv, dout,
+                            len(w.energies) * w.num_angles()))
+    torch.cuda.synchronize()
+    spat = sum(r[5] for r in stream_reqs)
+
+    def plain_stream():
+        t0 = time.perf_counter()
+        lat = []
+        for arrival, o, opt, dv, dout, _ in stream_reqs:
+            now = time.perf_counter() - t0
+            if now < arrival:
+                time.sleep(arrival - now)
+            _native.simulate_device(o, opt, dv.data_ptr(), dout.data_ptr(), cs.cuda_stream)
+            cs.synchronize()
+            lat.append(time.perf_counter() - t0 - arrival)
+        return time.perf_counter() - t0, lat
+
+    def served_stream(srv):
+        t0 = time.perf_counter()
+        ids = []
+        for arrival, o, opt, dv, dout, _ in stream_reqs:
+            now = time.perf_counter() - t0
+            if now < arrival:
+                time.sleep(arrival - now)
+            ids.append(srv.submit(o, opt, dv.data_ptr(), dout.data_ptr(), device=True))
+        lat = [srv.wait(i)[0] for i in ids]
+        return time.perf_counter() - t0, lat
+
+    plain_stream()
+    tps, lps = plain_stream()
+    with serving.Server(slots=args.slots) as srv:
+        served_stream(srv)
+        tss, lss = served_stream(srv)
+    mean_vox = sum(r[3].numel() // 4 for r in stream_reqs) / len(stream_reqs)
+    out["serving"] = {
+        "config": f"{len(stream_reqs)} requests, Poisson arrivals at 200/s (seeded); volume log-uniform in "
+                  "[32x128^2, 128x512^2] (FFT-friendly sizes), 2-4 materials, 1-100 energies, 6-36 E angles; "
+                  f"device-resident morphologies (mean {mean_vox / 1e6:.1f} M voxels x materials)",
+        "requests": len(stream_reqs), "patterns": spat, "arrival_span_s": stream_reqs[-1][0],
+        "plain": {"patterns_per_s": spat / tps, "seconds": tps, **_lat_summary(lps)},
+        "served": {"patterns_per_s": spat / tss, "seconds": tss, "slots": args.slots, **_lat_summary(lss)},
+        "speedup": tps / tss,
+    }
+    del stream_reqs
+    torch.cuda.empty_cache()
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -262,6 +409,10 @@ def main():
     if world != args.gpus:
         print(f"warning: --gpus {args.gpus} but WORLD_SIZE {world}", file=sys.stderr)
     torch.cuda.set_device(local)
+    if args.served_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "served": served_benchmarks(args)}), flush=True)
+        return 0
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -414,6 +565,10 @@ def main():
         result["precision"] = {"max_rel_err_vs_fp64": err, "pixels": npx,
                                "nan_mask_equal": bool(np.array_equal(np.isnan(gpu2), np.isnan(ref2))),
                                "sample": "1 energy x 2 E angles, full-size morphology, pixels above 1e-6 of peak"}
+    if rank == 0 and world == 1 and not args.skip_served:
+        del host_vox, host_vox_np
+        torch.cuda.empty_cache()
+        result["served"] = served_benchmarks(args)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if dist is not None:

@@ -69,6 +69,59 @@ def workload(name: str, energies=None) -> Workload:
     raise ValueError(f"unknown workload {name}")
 
 
+def batched_set(seed: int = 3) -> list:
+    """The batched configuration: 64 seeded two-phase morphologies of uneven
+    sizes, X = Y in {64, 128, 256} and Z in {16, 32, 64}, each with 20
+    energies (280-290 eV) and 12 E angles (0:15:165), physSize 5 nm."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    es = [float(e) for e in np.linspace(280.0, 290.0, 20)]
+    out = []
+    for i in range(64):
+        xy = int(rng.choice([64, 128, 256]))
+        z = int(rng.choice([16, 32, 64]))
+        out.append(Workload(f"batched_{i}", z, xy, xy, 2, es, (0.0, 165.0, 15.0), 5.0, seed=1000 + i))
+    return out
+
+
+def _smooth_sizes(lo: int, hi: int) -> list:
+    """FFT-friendly sizes (2^a 3^b 5^c 7^d) in [lo, hi]."""
+    out = []
+    for n in range(lo, hi + 1):
+        m = n
+        for p in (2, 3, 5, 7):
+            while m % p == 0:
+                m //= p
+        if m == 1:
+            out.append(n)
+    return out
+
+
+def serving_stream(n_requests: int, rate: float = 200.0, seed: int = 5) -> list:
+    """The serving configuration: Poisson arrivals (mean `rate` per second) of
+    requests whose volume is log-uniform between 32 x 128^2 and 128 x 512^2
+    voxels, quantised to FFT-friendly sizes, with 2-4 materials, 1-100
+    energies and 6-36 E angles.  Returns [(arrival_s, Workload)].  (Sizes with
+    prime factors above 7 are rejected by the engine, so none are drawn.)"""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xy_sizes = _smooth_sizes(128, 512)
+    z_sizes = _smooth_sizes(32, 128)
+    t, out = 0.0, []
+    for i in range(n_requests):
+        t += float(rng.exponential(1.0 / rate))
+        vol = math.exp(rng.uniform(math.log(32 * 128 * 128), math.log(128 * 512 * 512)))
+        # split the volume between Z (a quarter of the XY side, as in the bounds) and X = Y
+        side = (4.0 * vol) ** (1.0 / 3.0)
+        xy = min(xy_sizes, key=lambda n: abs(math.log(n / side)))
+        z = min(z_sizes, key=lambda n: abs(math.log(n / max(32.0, min(128.0, vol / (xy * xy))))))
+        m = int(rng.integers(2, 5))
+        ne = int(rng.integers(1, 101))
+        na = int(rng.integers(6, 37))
+        inc = 180.0 / na
+        es = [float(e) for e in np.linspace(270.0, 300.0, ne)] if ne > 1 else [285.0]
+        out.append((t, Workload(f"serve_{i}", z, xy, xy, m, es, (0.0, inc * (na - 1), inc), 2.0, seed=2000 + i)))
+    return out
+
+
 def optical_constants(w: Workload) -> np.ndarray:
     """[E][M][4] float32."""
     out = np.zeros((len(w.energies), w.num_material, 4), np.float64)
