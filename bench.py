@@ -292,21 +292,24 @@ def served_benchmarks(args):
     out = {}
     cs = torch.cuda.current_stream()
     # ---- batched: 64 uneven morphologies ----
-    reqs = []
+    reqs, per_energy_opts = [], []
     for w in workloads.batched_set():
         dv = workloads.voxels_torch(w).contiguous()
         hv = pinned((w.num_material, w.nz, w.ny, w.nx, 4))
         hv[...] = dv.cpu().numpy()
+        per_energy_opts.append(opts_for(w, strategy=1))
         reqs.append((opts_for(w), workloads.optical_constants(w), dv,
                      torch.empty(len(w.energies) * w.ny * w.nx, dtype=torch.float32, device="cuda"), hv,
                      pinned((len(w.energies), 1, w.ny, w.nx)), len(w.energies) * w.num_angles()))
     torch.cuda.synchronize()
     patterns = sum(r[6] for r in reqs)
 
-    def plain_batch(host):
+    def plain_batch(host, strategies=None):
         t0 = time.perf_counter()
         lat = []
-        for o, opt, dv, dout, hv, hout, _ in reqs:
+        for i, (o, opt, dv, dout, hv, hout, _) in enumerate(reqs):
+            if strategies is not None:
+                o = strategies[i]
             if host:
                 _native.cuda_main(o, opt, hv, out=hout)
             else:
@@ -344,6 +347,14 @@ def served_benchmarks(args):
                        **_lat_summary(ls)},
             "speedup": tp / ts,
         }
+        if not host:
+            # the share of the gain that is algorithmic: plain with the reference's per-energy schedule
+            plain_batch(False, per_energy_opts)
+            tpe, lpe = plain_batch(False, per_energy_opts)
+            out[name]["plain_per_energy"] = {"patterns_per_s": patterns / tpe, "seconds": tpe, **_lat_summary(lpe),
+                                             "note": "strategy PER_ENERGY (spectra per energy, as the reference "
+                                                     "schedules the path), one request at a time"}
+            out[name]["speedup_vs_per_energy"] = tpe / ts
     del reqs
     # ---- serving: Poisson stream, device-resident morphologies ----
     stream_reqs = []
