@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "c2", "z64", "c1", "small"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "c2", "c4", "z64", "c1", "small"])
     ap.add_argument("--energies-per-step", type=int, default=ENERGIES_PER_STEP)
     ap.add_argument("--strategy", type=int, default=0, choices=[0, 1, 2],
                     help="0 auto, 1 per-energy spectra, 2 field spectra once per request")
@@ -513,7 +513,7 @@ def main():
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded morphology with the configuration's shapes and distributions)",
         "config": {"workload": f"{w.name}: Z x Y x X = {w.nz} x {w.ny} x {w.nx}, {w.num_material} materials (Euler), "
-                               f"{nang} E angles (0:5:175), {len(energies)} energies per step per GPU, physSize "
+                               f"{nang} E angles ({w.angles[0]:g}:{w.angles[2]:g}:{w.angles[1]:g}), {len(energies)} energies per step per GPU, physSize "
                                f"{w.phys_size} nm, k = z",
                    "path": "plain (one request at a time, device-resident morphology)",
                    "l2": "inputs larger than L2 (morphology 4.3 GB)",

@@ -264,6 +264,8 @@ int setup_attrs(DeviceContext &ctx) {
   CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
 #define CYR_COLS_ATTR(V, T) \
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_COLS_ATTR(32, 8)
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_rows<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   CYR_COLS_ATTR(4, kColsTxY) CYR_COLS_ATTR(8, kColsTxY) CYR_COLS_ATTR(16, kColsTxY)
   CYR_COLS_ATTR(4, kColsTxZ) CYR_COLS_ATTR(8, kColsTxZ) CYR_COLS_ATTR(16, kColsTxZ)
 #undef CYR_COLS_ATTR
@@ -347,7 +349,9 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
       const dim3 grid(((nx + TX - 1) / TX) * cp.others, count);
       k_fft_cols<V, TX><<<grid, TX * 32, smem, st>>>(cp);
     };
-    if (axis == 1)
+    if (V == 32)  // 1024-point columns: 8 per block keeps the tile at 64 KB
+      launch(std::integral_constant<uint32_t, 8>{});
+    else if (axis == 1)
       launch(std::integral_constant<uint32_t, kColsTxY>{});
     else
       launch(std::integral_constant<uint32_t, kColsTxZ>{});
@@ -362,7 +366,8 @@ int warp_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, ui
   const uint32_t n = axis == 0 ? nx : axis == 1 ? ny : nz;
   if (n == 128) return warp_fft_pass_v<4>(ctx, data, nx, ny, nz, count, axis, st);
   if (n == 256) return warp_fft_pass_v<8>(ctx, data, nx, ny, nz, count, axis, st);
-  return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st);
+  if (n == 512) return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st);
+  return warp_fft_pass_v<32>(ctx, data, nx, ny, nz, count, axis, st);
 }
 
 // One y or z pass with k_fft_thread (lines of 8..64, one thread per line).
@@ -400,7 +405,7 @@ int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t n
   for (int axis = 0; axis < (skip_z ? 2 : 3); ++axis) {
     const uint32_t n = dims[axis];
     if (n == 1) continue;
-    if (n == 128 || n == 256 || n == 512) {
+    if (n == 128 || n == 256 || n == 512 || n == 1024) {
       CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st));
       continue;
     }

@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
 }
 
 // ---------------------------------------------------------------------------
-// Warp-level FFT for power-of-two lengths N = 32 V (V = 4, 8, 16).
+// Warp-level FFT for power-of-two lengths N = 32 V (V = 4, 8, 16, 32).
 //
 // One warp owns one line.  Lane t holds x[t + 32 i] in v[i] (natural order)
 // on entry and X[t + 32 i] on exit.  Each Stockham stage of radix R <= V runs
@@ -575,7 +575,7 @@ __host__ __device__ constexpr uint32_t line_stride(uint32_t n, uint32_t tx) {
 template <int V>
 struct WarpPlan {
   static constexpr int N = 32 * V;
-  static constexpr int LOG2N = V == 4 ? 7 : V == 8 ? 8 : 9;
+  static constexpr int LOG2N = V == 4 ? 7 : V == 8 ? 8 : V == 16 ? 9 : 10;
   // radices: as many 8s as V allows, then one 4 or 2 for the remainder
   static constexpr int MAXR = V >= 8 ? 8 : V;
   static constexpr int LOGMAXR = MAXR == 8 ? 3 : MAXR == 4 ? 2 : 1;

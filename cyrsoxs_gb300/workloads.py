@@ -12,6 +12,8 @@ benchmark configurations (no public dataset is involved).
   270-300 eV with 2 Lorentzian resonances per material; 36 E angles
   (0:5:175).  ``c2`` is 128 x 512 x 512 with physSize 2 nm; ``headline`` is
   the 512^2 x 256 shape (Z x Y x X = 256 x 512 x 512).
+* ``c4``: the large precision study, 3 materials on Z x Y x X = 256 x 1024 x
+  1024 with the same generators, 10 energies, 24 E angles (0:7.5:172.5).
 
 Arrays come back in the engine's layout: voxels float32 [M][Z][Y][X][4]
 (Euler s1 = (S, theta, psi, Vfrac)) and optical float32 [E][M][4]
@@ -64,6 +66,9 @@ def workload(name: str, energies=None) -> Workload:
     if name == "z64":  # the c2 physics on a 64 x 512 x 512 grid: a profiling size (about 3.5 GB on the device)
         es = energies or [float(e) for e in np.linspace(270.0, 300.0, 50)]
         return Workload("z64", 64, 512, 512, 4, es, (0.0, 175.0, 5.0), 2.0, 2, "random")
+    if name == "c4":  # large precision study: 3 materials on 256 x 1024 x 1024, 10 energies x 24 E angles
+        es = energies or [float(e) for e in np.linspace(270.0, 300.0, 10)]
+        return Workload("c4", 256, 1024, 1024, 3, es, (0.0, 172.5, 7.5), 2.0, 4, "random")
     if name == "small":
         return Workload("small", 16, 64, 64, 2, energies or [284.0, 286.0], (0.0, 150.0, 30.0), 5.0, 3, "random")
     raise ValueError(f"unknown workload {name}")

@@ -56,7 +56,8 @@ def rel_err(a, ref, thr=1e-6):
 @pytest.mark.parametrize("shape,count", [((4, 8, 16), 1), ((7, 15, 20), 2), ((1, 64, 48), 1), ((16, 32, 32), 3),
                                          ((32, 256, 256), 1), ((9, 25, 49), 1), ((3, 128, 512), 2),
                                          ((128, 20, 24), 1), ((256, 6, 40), 1), ((512, 512, 8), 1),
-                                         ((2, 512, 128), 3)])
+                                         ((2, 512, 128), 3), ((2, 8, 1024), 2), ((4, 1024, 24), 1), ((1024, 4, 40), 1),
+                                         ((16, 64, 40), 2), ((32, 8, 16), 1)])
 def test_fft3d_matches_numpy(shape, count):
     torch = _torch()
     nat = native()
