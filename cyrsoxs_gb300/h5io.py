@@ -579,7 +579,9 @@ def write_polarization(inp, p):
 
 
 def write_morphology_dump(inp, voxels: np.ndarray, dir_name: str = "Morphology"):
-    """Morphology/Morphology.h5 with Material_<m>/<component> [Z][Y][X] (writeH5.h:117-170)."""
+    """Morphology/Morphology.h5 with Material_<m>/<component> [Z][Y][X] and the
+    XDMF description Morphology/Morphology.xdmf that lets ParaView or VisIt
+    open it (writeH5.h:117-243)."""
     X, Y, Z = inp.voxelDims
     names = ("S", "Theta", "Psi", "Vfrac") if inp.morphologyType == 0 else ("Sx", "Sy", "Sz", "UnalignedFraction")
     v = np.asarray(voxels, np.float32).reshape(inp.NUM_MATERIAL, Z, Y, X, 4)
@@ -588,3 +590,23 @@ def write_morphology_dump(inp, voxels: np.ndarray, dir_name: str = "Morphology")
         for c, n in enumerate(names):
             ds[f"Material_{m + 1}/{n}"] = (np.ascontiguousarray(v[m, ..., c]), ["Z", "Y", "X"])
     write(os.path.join(dir_name, "Morphology.h5"), ds)
+    with open(os.path.join(dir_name, "Morphology.xdmf"), "w") as f:
+        f.write(_xdmf(names, inp.NUM_MATERIAL, (Z, Y, X)))
+
+
+def _xdmf(names, nmat, zyx):
+    dims = " ".join(str(n) for n in zyx)
+    attrs = []
+    for c in names:
+        for m in range(1, nmat + 1):
+            attrs.append(f'    <Attribute Name="Mat_{m}_{c}" AttributeType="Scalar" Center="Cell">\n'
+                         f'      <DataItem Dimensions="{dims}" NumberType="Float" Precision="4" Format="HDF">'
+                         f"Morphology.h5:/Material_{m}/{c}</DataItem>\n    </Attribute>\n")
+    return ('<?xml version="1.0" ?>\n<!DOCTYPE Xdmf SYSTEM "Xdmf.dtd" []>\n'
+            '<Xdmf xmlns:xi="http://www.w3.org/2003/XInclude" Version="2.2">\n <Domain>\n'
+            '  <Grid Name="morphology" GridType="Uniform">\n'
+            f'    <Topology TopologyType="3DCORECTMesh" NumberOfElements="{dims}"/>\n'
+            '    <Geometry GeometryType="ORIGIN_DXDYDZ">\n'
+            '      <DataItem Name="origin" Dimensions="3" NumberType="Float" Precision="4" Format="XML">0.0 0.0 0.0</DataItem>\n'
+            '      <DataItem Name="spacing" Dimensions="3" NumberType="Float" Precision="4" Format="XML">1.0 1.0 1.0</DataItem>\n'
+            '    </Geometry>\n' + "".join(attrs) + '  </Grid>\n </Domain>\n</Xdmf>\n')

@@ -111,3 +111,36 @@ def test_cli_without_a_gpu_fails_loudly(tmp_path, monkeypatch, capsys):
     assert cli.main(["morph.h5"]) == 1
     assert "no device" in capsys.readouterr().out
     assert cli.main([]) == 1
+
+
+def test_constants_interpolation_and_material_files(tmp_path):
+    from cyrsoxs_gb300 import constants
+
+    table = np.array([[280.0, 1e-3, 1e-4, 2e-3, 2e-4],
+                      [282.0, 3e-3, 3e-4, 4e-3, 4e-4],
+                      [282.0, 9e-3, 9e-4, 9e-3, 9e-4],   # duplicate energy: the first row is kept
+                      [281.0, 2e-3, 2e-4, 3e-3, 3e-4]])
+    c = constants.interpolate(table, [280.5, 282.0])
+    np.testing.assert_allclose(c[0], [1.5e-3, 1.5e-4, 2.5e-3, 2.5e-4])
+    np.testing.assert_allclose(c[1], [3e-3, 3e-4, 4e-3, 4e-4])
+    with pytest.raises(ValueError):
+        constants.interpolate(table, [279.0])
+    constants.write_material(str(tmp_path / "Material1.txt"), [280.5, 282.0], c)
+    constants.write_material(str(tmp_path / "Material2.txt"), [280.5, 282.0])  # vacuum
+    opt = config.read_materials(2, [280.5, 282.0], str(tmp_path))
+    np.testing.assert_allclose(opt[:, 0], c, rtol=1e-6)
+    assert not opt[:, 1].any()
+
+
+def test_morphology_dump_writes_h5_and_xdmf(tmp_path, monkeypatch):
+    from cyrsoxs_gb300 import CyRSoXS as cy
+
+    monkeypatch.chdir(tmp_path)
+    inp = cy.InputData(NumMaterial=2)
+    inp.setDimensions([2, 3, 4], cy.MorphologyOrder.ZYX)
+    vox = np.arange(2 * 24 * 4, dtype=np.float32).reshape(2, 24, 4)
+    h5io.write_morphology_dump(inp, vox)
+    f = h5io.File("Morphology/Morphology.h5")
+    np.testing.assert_array_equal(f.read("Material_2/Psi"), vox[1, :, 2].reshape(2, 3, 4))
+    x = open("Morphology/Morphology.xdmf").read()
+    assert 'NumberOfElements="2 3 4"' in x and "Morphology.h5:/Material_2/Vfrac" in x
