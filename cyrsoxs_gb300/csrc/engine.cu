@@ -322,14 +322,13 @@ int make_axis(DeviceContext &ctx, uint32_t n, FftAxis &ax) {
 // One axis of the 3D FFT with the warp-level kernels (n = 128, 256, 512).
 template <int V>
 int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
-                    cudaStream_t st) {
+                    cudaStream_t st, size_t nvox) {
   constexpr uint32_t N = 32 * V;
-  const size_t nvox = size_t(nx) * ny * nz;
   const float2 *tw = nullptr;
   CYR_TRY(get_twiddles(ctx, N, &tw));
   const int slot = ctx.prof.begin(axis == 0 ? kFftRows : axis == 1 ? kFftColsY : kFftColsZ, st);
   if (axis == 0) {
-    RowPassParams rp{data, uint32_t(size_t(ny) * nz * count), tw};
+    RowPassParams rp{data, uint32_t(size_t(ny) * nz * count), tw, ny * nz, nvox};
     const size_t smem = (N + 8 * N) * sizeof(float2);
     k_fft_rows<V><<<(rp.rows + 7) / 8, 256, smem, st>>>(rp);
   } else {
@@ -362,24 +361,24 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
 }
 
 int warp_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
-                  cudaStream_t st) {
+                  cudaStream_t st, size_t nvox) {
   const uint32_t n = axis == 0 ? nx : axis == 1 ? ny : nz;
-  if (n == 128) return warp_fft_pass_v<4>(ctx, data, nx, ny, nz, count, axis, st);
-  if (n == 256) return warp_fft_pass_v<8>(ctx, data, nx, ny, nz, count, axis, st);
-  if (n == 512) return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st);
-  return warp_fft_pass_v<32>(ctx, data, nx, ny, nz, count, axis, st);
+  if (n == 128) return warp_fft_pass_v<4>(ctx, data, nx, ny, nz, count, axis, st, nvox);
+  if (n == 256) return warp_fft_pass_v<8>(ctx, data, nx, ny, nz, count, axis, st, nvox);
+  if (n == 512) return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st, nvox);
+  return warp_fft_pass_v<32>(ctx, data, nx, ny, nz, count, axis, st, nvox);
 }
 
 // One y or z pass with k_fft_thread (lines of 8..64, one thread per line).
 int thread_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
-                    cudaStream_t st) {
+                    cudaStream_t st, size_t nvox) {
   const uint32_t n = axis == 1 ? ny : nz;
   const float2 *tw = nullptr;
   CYR_TRY(get_twiddles(ctx, n, &tw));
   ThreadPassParams p{};
   p.data = data;
   p.nx = nx;
-  p.vstride = size_t(nx) * ny * nz;
+  p.vstride = nvox;
   p.tw = tw;
   if (axis == 1) {
     p.others = nz, p.ostride = size_t(nx) * ny, p.estride = nx;
@@ -397,20 +396,23 @@ int thread_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
   return CYR_OK;
 }
 
-// In-place forward 3D FFT of `count` volumes.
-int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
-          bool skip_z = false) {
-  const size_t nvox = size_t(nx) * ny * nz;
+// In-place forward FFT of `count` volumes along the axes [first, last]
+// (0 x, 1 y, 2 z).  vstride (elements between volumes) defaults to the volume
+// size; a larger one runs the x and y passes on nz planes of larger volumes
+// (data pointing at the first plane), as the slab pipeline does.
+int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
+             int first, int last, size_t vstride = 0) {
+  const size_t nvox = vstride ? vstride : size_t(nx) * ny * nz;
   const uint32_t dims[3] = {nx, ny, nz};
-  for (int axis = 0; axis < (skip_z ? 2 : 3); ++axis) {
+  for (int axis = first; axis <= last; ++axis) {
     const uint32_t n = dims[axis];
     if (n == 1) continue;
     if (n == 128 || n == 256 || n == 512 || n == 1024) {
-      CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st));
+      CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st, nvox));
       continue;
     }
     if (axis > 0 && (n == 8 || n == 16 || n == 32 || n == 64) && count <= 65535) {
-      CYR_TRY(thread_fft_pass(ctx, data, nx, ny, nz, count, axis, st));
+      CYR_TRY(thread_fft_pass(ctx, data, nx, ny, nz, count, axis, st, nvox));
       continue;
     }
     FftPassParams p{};
@@ -437,6 +439,11 @@ int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t n
     CYR_CUDA(cudaGetLastError());
   }
   return CYR_OK;
+}
+
+int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
+          bool skip_z = false) {
+  return fft_axes(ctx, data, nx, ny, nz, count, st, 0, skip_z ? 1 : 2);
 }
 
 // ---------------------------------------------------------------------------
@@ -876,10 +883,57 @@ EwaldParams ewald_params(const Plan &pl, const cyr_options *o, const unsigned ch
   return p;
 }
 
+// Slab upload of a host morphology (FIELDS strategy): events[s] completes when
+// planes [s * planes, (s + 1) * planes) of every material are on the device.
+// Slabs are issued one ahead of the compute that needs them: from pageable
+// memory a copy call returns only once its data is staged, so the kernels of
+// the previous slab must already be queued for the two to overlap.
+struct SlabUpload {
+  uint32_t planes = 0, count = 0, issued = 0;
+  std::vector<cudaEvent_t> events;
+  // every sample_zstep-th plane, copied first for the means (a sample spread over the volume)
+  uint32_t sample_zstep = 1;
+  cudaEvent_t sample = nullptr;
+  const float *host = nullptr;
+  float4 *dev = nullptr;
+  uint32_t nmat = 0, nz = 0;
+  size_t nvox = 0, npix = 0;
+  cudaStream_t stream = nullptr;
+  int issue(uint32_t s) {  // queues the copies of slabs up to s
+    for (; issued <= s && issued < count; ++issued) {
+      const uint32_t z0 = issued * planes, z1 = std::min(nz, z0 + planes);
+      for (uint32_t m = 0; m < nmat; ++m) {
+        const size_t off = size_t(m) * nvox + size_t(z0) * npix;  // float4 elements
+        CYR_CUDA(cudaMemcpyAsync(dev + off, host + 4 * off, size_t(z1 - z0) * npix * sizeof(float4),
+                                 cudaMemcpyHostToDevice, stream));
+      }
+      cudaEvent_t ev = nullptr;
+      CYR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      events.push_back(ev);
+      CYR_CUDA(cudaEventRecord(ev, stream));
+    }
+    return CYR_OK;
+  }
+  int issue_sample() {
+    const size_t pitch = size_t(sample_zstep) * npix * sizeof(float4);
+    for (uint32_t m = 0; m < nmat; ++m)
+      CYR_CUDA(cudaMemcpy2DAsync(dev + size_t(m) * nvox, pitch, host + 4 * size_t(m) * nvox, pitch,
+                                 npix * sizeof(float4), (nz + sample_zstep - 1) / sample_zstep,
+                                 cudaMemcpyHostToDevice, stream));
+    CYR_CUDA(cudaEventCreateWithFlags(&sample, cudaEventDisableTiming));
+    CYR_CUDA(cudaEventRecord(sample, stream));
+    return CYR_OK;
+  }
+  ~SlabUpload() {
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+    if (sample) cudaEventDestroy(sample);
+  }
+};
+
 // FIELDS strategy after the moments: field means, packed field spectra, then
 // every energy (in batches) and k from them.
 int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan &pl, const unsigned char *dp,
-               const float4 *d_vox, float *d_out, cudaStream_t st) {
+               const float4 *d_vox, float *d_out, cudaStream_t st, size_t nsamp, const SlabUpload *up) {
   const uint32_t npk = pl.npk;
   CYR_TRY(sc.spec.ensure(size_t(npk) * pl.nvox * sizeof(float2)));
   CYR_TRY(sc.images.ensure(size_t(pl.ebatch) * image_bytes(pl)));
@@ -890,7 +944,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   fp.nx = pl.nx, fp.ny = pl.ny, fp.nz = pl.nz, fp.nmat = pl.nmat;
   fp.nvox = pl.nvox;
   fp.mom = sc.moments.as<double>();  // each block forms the field means from the moments
-  fp.nsamp = pl.npix * ((pl.nz + pl.mom_zstep - 1) / pl.mom_zstep);
+  fp.nsamp = nsamp;
   if (pl.hanning) {
     fp.hann_x = reinterpret_cast<const float *>(dp + pl.off_hx);
     fp.hann_y = reinterpret_cast<const float *>(dp + pl.off_hy);
@@ -899,15 +953,28 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   fp.out = spec;
   int sms = 0;
   CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
-  const uint32_t blocks = uint32_t(std::min<size_t>((pl.nvox + 255) / 256, size_t(sms) * 8));
-  int slot = ctx.prof.begin(kBuildFields, st);
-  if (o->morphology_type == 0)
-    k_build_fields<0><<<blocks, 256, 0, st>>>(fp);
-  else
-    k_build_fields<1><<<blocks, 256, 0, st>>>(fp);
-  ctx.prof.end(slot, st);
-  CYR_CUDA(cudaGetLastError());
-  CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st));
+  // fields of planes [z0, z1), then their x and y passes (the axes commute; z comes last)
+  const uint32_t step = up ? up->planes : pl.nz, nslab = up ? up->count : 1;
+  for (uint32_t sl = 0; sl < nslab; ++sl) {
+    const uint32_t z0 = sl * step, z1 = std::min(pl.nz, z0 + step);
+    if (up) {
+      CYR_TRY(const_cast<SlabUpload *>(up)->issue(sl));
+      CYR_CUDA(cudaStreamWaitEvent(st, up->events[sl], 0));
+    }
+    fp.i0 = size_t(z0) * pl.npix, fp.i1 = size_t(z1) * pl.npix;
+    const uint32_t blocks = uint32_t(std::min<size_t>((fp.i1 - fp.i0 + 255) / 256, size_t(sms) * 8));
+    int slot = ctx.prof.begin(kBuildFields, st);
+    if (o->morphology_type == 0)
+      k_build_fields<0><<<blocks, 256, 0, st>>>(fp);
+    else
+      k_build_fields<1><<<blocks, 256, 0, st>>>(fp);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+    CYR_TRY(fft_axes(ctx, spec + fp.i0, pl.nx, pl.ny, z1 - z0, npk, st, 0, 1, pl.nvox));
+    if (up) CYR_TRY(const_cast<SlabUpload *>(up)->issue(sl + 1));  // the next slab's copy, behind this slab's kernels
+  }
+  CYR_TRY(fft_axes(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st, 2, 2));
+  int slot = -1;
 
   FieldEwaldParams fe{};
   fe.zspec = spec;  // every Ewald block forms the DC replacement of each packed volume
@@ -1001,7 +1068,13 @@ struct RunMode {
   size_t host_arena_bytes = 0;
   bool capturing = false;
   const Plan *plan = nullptr;  // made by the caller for these options (strategy resolved), or null
+  // host morphology to upload into d_vox first: with the FIELDS strategy in
+  // z slabs on copy_stream, each slab's fields built and x/y-transformed as
+  // soon as it lands, so the upload hides most of the transform
+  const float *host_vox = nullptr;
+  cudaStream_t copy_stream = nullptr;
 };
+
 
 int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const float *optical, const float4 *d_vox,
                 float *d_out, cudaStream_t st, const RunMode &mode = RunMode()) {
@@ -1036,6 +1109,27 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
     CYR_CUDA(cudaMemcpyAsync(sc.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
   }
   const unsigned char *dp = sc.params.as<unsigned char>();
+  // host morphology: uploaded in z slabs (FIELDS) or at once (per-energy spectra)
+  SlabUpload upload;
+  if (mode.host_vox) {
+    upload.stream = mode.copy_stream ? mode.copy_stream : st;
+    if (upload.stream != st) CYR_CUDA(cudaStreamWaitEvent(upload.stream, sc.last_use, 0));
+    upload.host = mode.host_vox;
+    upload.dev = const_cast<float4 *>(d_vox);
+    upload.nmat = pl.nmat, upload.nz = pl.nz, upload.nvox = pl.nvox, upload.npix = pl.npix;
+    upload.count = pl.fields && pl.nz >= 8 ? 8u : 1u;
+    upload.planes = (pl.nz + upload.count - 1) / upload.count;
+    upload.count = (pl.nz + upload.planes - 1) / upload.planes;
+    if (pl.fields) {
+      upload.sample_zstep = std::max(1u, pl.nz / 8);
+      CYR_TRY(upload.issue_sample());
+      CYR_TRY(upload.issue(0));
+    } else {
+      CYR_TRY(upload.issue(upload.count - 1));
+      CYR_CUDA(cudaStreamWaitEvent(st, upload.events.back(), 0));
+    }
+  }
+  const bool slabs = mode.host_vox && pl.fields;
   // volume moments of the morphology -> mean of every tensor entry, per energy
   CYR_TRY(sc.moments.ensure(size_t(pl.nmat) * kMoments * sizeof(double)));
   CYR_TRY(sc.means.ensure(size_t(pl.ne) * 6 * sizeof(float2)));
@@ -1058,7 +1152,12 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
     mp.out = sc.moments.as<double>();
     mp.conv = convert ? sc.conv.as<float4>() : nullptr;
     // the conversion needs every voxel; the means alone need only a subsample of planes
+    // (with a slab upload: the planes copied first for that purpose)
     mp.zstep = convert ? 1u : pl.mom_zstep;
+    if (slabs) {
+      mp.zstep = upload.sample_zstep;
+      CYR_CUDA(cudaStreamWaitEvent(st, upload.sample, 0));
+    }
     mp.neg = sc.flags.as<unsigned>();
     int nsm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx.device));
@@ -1074,7 +1173,8 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
     if (pl.fields) {
-      CYR_TRY(run_fields(ctx, sc, o, pl, dp, d_vox, d_out, st));
+      const size_t nsamp = pl.npix * ((mp.nz + mp.zstep - 1) / mp.zstep);
+      CYR_TRY(run_fields(ctx, sc, o, pl, dp, d_vox, d_out, st, nsamp, slabs ? &upload : nullptr));
       // an event recorded inside a capture cannot be waited on outside it (slots keep order by their stream)
       if (!mode.capturing) CYR_CUDA(cudaEventRecord(sc.last_use, st));
       return CYR_OK;
@@ -1743,15 +1843,19 @@ static int cuda_main_impl(const cyr_options *opt, const float *optical, const fl
   const size_t out_bytes = size_t(o.num_energies) * nk * o.nx * o.ny * sizeof(float);
   CYR_TRY(ctx->vox_in.ensure(vox_bytes));
   CYR_TRY(ctx->out_in.ensure(out_bytes));
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr, cs = nullptr;
   CYR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(st);
+    return fail(CYR_ERR_CUDA, "stream creation failed");
+  }
   int rc = CYR_OK;
   do {
-    if (cudaMemcpyAsync(ctx->vox_in.ptr, voxels, vox_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
-      rc = fail(CYR_ERR_CUDA, "voxel upload failed: %s", cudaGetErrorString(cudaGetLastError()));
-      break;
-    }
-    rc = run_request(*ctx, ctx->main, &o, optical, ctx->vox_in.as<float4>(), ctx->out_in.as<float>(), st);
+    // the morphology is uploaded by run_request, overlapped with the field transform (FIELDS)
+    RunMode mode;
+    mode.host_vox = voxels;
+    mode.copy_stream = cs;
+    rc = run_request(*ctx, ctx->main, &o, optical, ctx->vox_in.as<float4>(), ctx->out_in.as<float>(), st, mode);
     if (rc != CYR_OK) break;
     if (cudaMemcpyAsync(projection, ctx->out_in.ptr, out_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
       rc = fail(CYR_ERR_CUDA, "projection download failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -1766,6 +1870,8 @@ static int cuda_main_impl(const cyr_options *opt, const float *optical, const fl
     if (cudaMemcpy(&errs, ctx->main.errors.ptr, sizeof errs, cudaMemcpyDeviceToHost) == cudaSuccess && errs != 0)
       rc = fail(CYR_ERR_CUDA, "%u detector pixels needed z planes outside the kept range", errs);
   } while (false);
+  cudaStreamSynchronize(cs);
+  cudaStreamDestroy(cs);
   cudaStreamDestroy(st);
   return rc;
 }

@@ -63,6 +63,7 @@ struct FieldParams {
   size_t nvox;
   const double *mom;     // [nmat][kMoments] moment sums over nsamp voxels
   size_t nsamp;
+  size_t i0, i1;         // voxels built: [i0, i1) (whole z planes)
   const float *hann_x, *hann_y, *hann_z;  // null when no windowing
   float2 *out;           // [num_packed][nvox]: field 2j in .x, field 2j+1 in .y
 };
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
   field_means(p.mom, p.nmat, p.nsamp, mean);
   __syncthreads();
   const size_t stride = size_t(gridDim.x) * blockDim.x;
-  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.nvox; i += stride) {
+  for (size_t i = p.i0 + size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.i1; i += stride) {
     float w = 1.f;
     if (p.hann_x) {
       const uint32_t x = uint32_t(i % p.nx), y = uint32_t((i / p.nx) % p.ny), z = uint32_t(i / (size_t(p.nx) * p.ny));

@@ -666,8 +666,10 @@ __device__ __forceinline__ void warp_fft(float2 (&v)[V], float2 *line, const flo
 // Row pass (x axis): one warp per contiguous row, straight from and to HBM.
 struct RowPassParams {
   float2 *data;
-  uint32_t rows;   // rows in all volumes
+  uint32_t rows;       // rows in all volumes
   const float2 *tw;
+  uint32_t rows_per_vol;
+  size_t vstride;      // elements between volumes
 };
 
 template <int V>
@@ -681,7 +683,7 @@ __global__ void __launch_bounds__(256) k_fft_rows(RowPassParams p) {
   __syncthreads();
   const uint32_t row = blockIdx.x * (blockDim.x >> 5) + warp;
   if (row >= p.rows) return;
-  float2 *r = p.data + size_t(row) * N;
+  float2 *r = p.data + size_t(row / p.rows_per_vol) * p.vstride + size_t(row % p.rows_per_vol) * N;
   float2 v[V];
 #pragma unroll
   for (int i = 0; i < V; ++i) v[i] = r[lane + 32 * i];
