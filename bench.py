@@ -165,7 +165,7 @@ def algorithmic_bytes(kernel, w, nvol, nang, planes, batch=1, npk=0):
     strategy nvol = packed field volumes, batch = energies per Ewald/rotation launch."""
     V, P, M = w.nvox, w.nx * w.ny, w.num_material
     if npk:
-        nq = 16 * (2 if nvol == 6 else 1)  # Gram map bytes per pixel
+        nq = 4 * (6 if nvol == 6 else 3)  # Gram bytes per pixel and energy (packed records)
         table = {
             "k_build_fields": (16 * M + 8 * npk) * V,
             "k_moments": 16 * M * P * math.ceil(w.nz / max(1, w.nz // 16)),  # every (nz / 16)-th z plane

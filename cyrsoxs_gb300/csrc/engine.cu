@@ -479,19 +479,30 @@ struct Plan {
   uint32_t ebatch = 1;                  // energies per Ewald / rotation launch
   size_t off_fcoef = 0, off_kmag = 0, off_mat = 0;
   uint32_t mom_zstep = 1;               // z planes between the moment samples (FIELDS)
+  // LAB frame, square detector: conservative per-row column ranges of the
+  // Ewald output, [k][energy][row] (ewald_rows)
+  bool has_rows = false;
+  size_t off_rows = 0;
 };
 
-// Bytes of one energy's Ewald output: Gram maps in the LAB frame (rotated by
-// k_rotate_gram), per-angle images in the MATERIAL frame (k_rotate_average).
-size_t image_bytes(const Plan &pl) {
-  if (pl.material_frame) return size_t(pl.nang) * pl.npix * sizeof(float);
-  return pl.npix * sizeof(float4) * (pl.nbasis == 3 ? 2 : 1);
+// Energies per Gram record: the FIELDS strategy packs 12 floats per pixel (4
+// energies with 2 bases, 2 with 3); the per-energy path keeps one.
+inline uint32_t gram_nep(const Plan &pl) { return pl.fields && !pl.material_frame ? (pl.nbasis == 2 ? 4u : 2u) : 1u; }
+
+// Bytes of the Ewald output of nb energies: Gram records in the LAB frame
+// (rotated by k_rotate_gram), per-angle images in the MATERIAL frame
+// (k_rotate_average).
+size_t image_bytes(const Plan &pl, uint32_t nb = 1) {
+  if (pl.material_frame) return size_t(nb) * pl.nang * pl.npix * sizeof(float);
+  const uint32_t nep = gram_nep(pl), ng = pl.nbasis * (pl.nbasis + 1) / 2;
+  const size_t rq = (size_t(nep) * ng + 3) / 4;
+  return size_t((nb + nep - 1) / nep) * pl.npix * rq * sizeof(float4);
 }
 
 // Device bytes of the FIELDS strategy: packed field spectra, per-batch images and averages.
 size_t field_bytes(const Plan &pl) {
-  return size_t(pl.npk) * pl.nvox * sizeof(float2) + size_t(pl.ebatch) * (image_bytes(pl) + pl.npix * sizeof(float)) +
-         pl.arena.size() + (num_fields(pl.nmat) + 2 * pl.npk) * sizeof(float2);
+  return size_t(pl.npk) * pl.nvox * sizeof(float2) + image_bytes(pl, pl.ebatch) +
+         size_t(pl.ebatch) * pl.npix * sizeof(float) + pl.arena.size() + (num_fields(pl.nmat) + 2 * pl.npk) * sizeof(float2);
 }
 
 // Dynamic shared memory of k_build_fft_z_warp: twiddles, lines, optional tile.
@@ -560,6 +571,42 @@ size_t arena_put(std::vector<unsigned char> &a, const T *src, size_t count) {
   a.resize(off + sizeof(T) * count);
   if (count) std::memcpy(a.data() + off, src, sizeof(T) * count);
   return off;
+}
+
+// Column ranges of the Ewald output that can hold a number, per k, energy and
+// detector row (LAB frame, square detector, where the rotation's image row y
+// is detector row Y).  ewald_geometry marks a pixel NaN unless
+// val = k^2 - (kx + qx)^2 - (ky + qy)^2 >= 0, so outside the disc
+// |kx + qx| <= sqrt(k^2 - (ky + qy)^2) the pixel is NaN.  The bound takes val
+// down to -1e-5 k^2 and adds two columns on each side, far beyond the float
+// rounding of the device's test; a row with no such column stores [W, -1].
+void ewald_rows(const cyr_options *o, Plan &pl) {
+  pl.has_rows = !pl.material_frame && pl.nx == pl.ny && size_t(pl.nx) * sizeof(int2) <= 48 * 1024;
+  if (!pl.has_rows) return;
+  const int W = int(pl.ny), H = int(pl.nx);
+  const float start = -static_cast<float>(kPi / o->phys_size);
+  const float dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.ny - 1) * 1.0));
+  const float dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nx - 1) * 1.0));
+  std::vector<int2> rows(size_t(pl.nk) * pl.ne * H);
+  for (uint32_t k = 0; k < pl.nk; ++k)
+    for (uint32_t e = 0; e < pl.ne; ++e) {
+      const float kmag = static_cast<float>(2 * kPi / static_cast<float>(1239.84197 / o->energies[e]));
+      const double kx = double(kmag * pl.frames[k].k.x), ky = double(kmag * pl.frames[k].k.y);
+      for (int Y = 0; Y < H; ++Y) {
+        int lo = W, hi = -1;
+        const double ay = ky + double(start + float(Y) * dy);
+        const double r2 = double(kmag) * kmag * (1.0 + 1e-5) - ay * ay;
+        if (r2 >= 0) {
+          const double r = std::sqrt(r2);
+          const double xl = (-kx - r - double(start)) / double(dx), xh = (-kx + r - double(start)) / double(dx);
+          lo = int(std::max(0.0, std::floor(xl) - 2.0));
+          hi = int(std::min(double(W - 1), std::ceil(xh) + 2.0));
+          if (hi < lo) lo = W, hi = -1;
+        }
+        rows[(size_t(k) * pl.ne + e) * H + Y] = int2{lo, hi};
+      }
+    }
+  pl.off_rows = arena_put(pl.arena, rows.data(), rows.size());
 }
 
 // make_kframe scans 100 000 candidate base angles (as the reference does per
@@ -774,9 +821,15 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
     pl.fields = o->strategy == CYR_STRATEGY_FIELDS;
   }
   {
-    // per energy: Gram maps (LAB) or per-angle images (MATERIAL), kept within L2 for the rotation
-    const size_t img = image_bytes(pl);
-    pl.ebatch = uint32_t(std::max<size_t>(1, std::min<size_t>({size_t(pl.ne), size_t(32), (size_t(96) << 20) / img})));
+    // energies per Ewald / rotation launch: their Gram records (LAB) or
+    // per-angle images (MATERIAL) stay within L2 for the rotation; batches of
+    // even size, each a whole number of records
+    const uint32_t nep = gram_nep(pl), cap = std::min<uint32_t>(pl.ne, 32);
+    uint32_t emax = 1;
+    while (emax < cap && image_bytes(pl, emax + 1) <= (size_t(96) << 20)) ++emax;
+    const uint32_t nbatches = (pl.ne + emax - 1) / emax;
+    const uint32_t eb = (pl.ne + nbatches - 1) / nbatches;
+    pl.ebatch = nbatches == 1 ? pl.ne : std::min(pl.ne, (eb + nep - 1) / nep * nep);
   }
   if (pl.fields) {
     pl.mom_zstep = std::max(1u, pl.nz / 16);  // 16 sampled planes
@@ -840,6 +893,7 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
     }
     pl.off_mat = arena_put(pl.arena, mat.data(), mat.size());
   }
+  ewald_rows(o, pl);
   pl.arena.resize((pl.arena.size() + 255) & ~size_t(255));
   return CYR_OK;
 }
@@ -936,7 +990,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
                const float4 *d_vox, float *d_out, cudaStream_t st, size_t nsamp, const SlabUpload *up) {
   const uint32_t npk = pl.npk;
   CYR_TRY(sc.spec.ensure(size_t(npk) * pl.nvox * sizeof(float2)));
-  CYR_TRY(sc.images.ensure(size_t(pl.ebatch) * image_bytes(pl)));
+  CYR_TRY(sc.images.ensure(image_bytes(pl, pl.ebatch)));
   CYR_TRY(sc.avg.ensure(size_t(pl.ebatch) * pl.npix * sizeof(float)));
   float2 *spec = sc.spec.as<float2>();
   FieldParams fp{};
@@ -1024,10 +1078,15 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
     rg.nangles = pl.nang;
     rg.rot_mask = o->rot_mask;
     rg.avg = rp.avg;
+    const uint32_t nep = gram_nep(pl);
+    const size_t rsm = pl.has_rows ? size_t(H) * sizeof(int2) : 0;
     for (uint32_t e0 = 0; e0 < pl.ne; e0 += pl.ebatch) {
       const uint32_t nb = std::min(pl.ebatch, pl.ne - e0);
       fe.e0 = e0;
       fe.nbatch = nb;
+      rg.nenergies = nb;
+      rg.rows = pl.has_rows ? reinterpret_cast<const int2 *>(dp + pl.off_rows) + (size_t(k) * pl.ne + e0) * H : nullptr;
+      const dim3 rgrid(rot_tiles, (nb + nep - 1) / nep);
       slot = ctx.prof.begin(kEwaldFields, st);
       const unsigned fgrid = fpix_blocks * nb;
       if (pl.material_frame)
@@ -1041,9 +1100,9 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
       if (pl.material_frame)
         k_rotate_average<<<dim3(pix_blocks, nb), 256, 0, st>>>(rp);
       else if (pl.nbasis == 2)
-        k_rotate_gram<2><<<dim3(rot_tiles, nb), kRotTile * kRotTile, 0, st>>>(rg);
+        k_rotate_gram<2, packed_energies<2>()><<<rgrid, kRotTile * kRotTile, rsm, st>>>(rg);
       else
-        k_rotate_gram<3><<<dim3(rot_tiles, nb), kRotTile * kRotTile, 0, st>>>(rg);
+        k_rotate_gram<3, packed_energies<3>()><<<rgrid, kRotTile * kRotTile, rsm, st>>>(rg);
       ctx.prof.end(slot, st);
       float *dst = d_out + (size_t(e0) * pl.nk + k) * pl.npix;
       slot = ctx.prof.begin(kFill, st);
@@ -1408,12 +1467,15 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
         rg.ecoef = dcoef + size_t(k) * pl.nang * pl.nbasis;
         rg.W = W, rg.H = H;
         rg.nangles = pl.nang;
+        rg.nenergies = 1;
         rg.rot_mask = o->rot_mask;
         rg.avg = avg;
+        rg.rows = pl.has_rows ? reinterpret_cast<const int2 *>(dp + pl.off_rows) + (size_t(k) * pl.ne + e) * H : nullptr;
+        const size_t rsm = pl.has_rows ? size_t(H) * sizeof(int2) : 0;
         if (pl.nbasis == 2)
-          k_rotate_gram<2><<<rot_tiles, kRotTile * kRotTile, 0, st>>>(rg);
+          k_rotate_gram<2, 1><<<rot_tiles, kRotTile * kRotTile, rsm, st>>>(rg);
         else
-          k_rotate_gram<3><<<rot_tiles, kRotTile * kRotTile, 0, st>>>(rg);
+          k_rotate_gram<3, 1><<<rot_tiles, kRotTile * kRotTile, rsm, st>>>(rg);
       }
       ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());

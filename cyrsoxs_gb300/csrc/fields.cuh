@@ -134,7 +134,7 @@ struct FieldEwaldParams {
   const float *mat;      // NB = 0: [nangles][3][6]
   const float *ecoef;    // NB > 0: [nangles][NB] E components of the LAB angle basis
   float *images;         // NB = 0: [batch][nangles][npix]
-  float4 *gram;          // NB > 0: Gram maps [batch][npix][NQ]
+  float4 *gram;          // NB > 0: Gram records [batch / NEP][npix][RQ] (GramRec<NB, packed_energies<NB>()>)
   uint32_t nbatch;       // energies of this launch
 };
 
@@ -167,11 +167,14 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   float w1;
   int nplanes;
   float *img = p.images + size_t(eb) * p.nangles * npix + t;
-  constexpr int NBG = NB > 0 ? NB : 1;
-  float4 *gm = p.gram + (size_t(eb) * npix + t) * GramLayout<NBG>::NQ;
+  constexpr int NBG = NB > 0 ? NB : 1, NEP = packed_energies<NBG>();
+  constexpr int NGG = GramRec<NBG, NEP>::NG;
+  float *gm = reinterpret_cast<float *>(p.gram + (size_t(eb / NEP) * npix + t) * GramRec<NBG, NEP>::RQ) +
+              (eb % NEP) * NGG;
   if (!ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes)) {
     if constexpr (NB > 0) {
-      gram_store_nan<NB>(gm);
+#pragma unroll
+      for (int q = 0; q < NGG; ++q) gm[q] = __int_as_float(0x7fc00000);
     } else {
       const float nanv = __int_as_float(0x7fc00000);
       for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
@@ -242,7 +245,8 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
     }
   }
   if constexpr (NB > 0) {
-    gram_store<NB>(gm, G);
+#pragma unroll
+    for (int q = 0; q < NGG; ++q) gm[q] = G[q];
   } else {
     const float w0 = 1.f - w1;
     for (uint32_t a = 0; a < p.nangles; ++a) {

@@ -1204,7 +1204,7 @@ struct WarpCoef {
 // Source corners and fractions of destination pixel (xd, yd); false when the
 // source point lies outside the image (the destination keeps its value).
 struct WarpTap {
-  int i00, i01, i10, i11;  // y0 x0, y0 x1, y1 x0, y1 x1 (row-major, width W)
+  int x0, x1, y0, y1;  // corner columns and rows (row-major image, width W)
   float fx, fy;
 };
 
@@ -1215,7 +1215,7 @@ __device__ __forceinline__ bool warp_tap(int W, int H, const WarpCoef &c, int xd
   if (!(xs >= 0.f && xs <= float(W - 1) && ys >= 0.f && ys <= float(H - 1))) return false;
   const int x0 = min(int(floorf(xs)), W - 1), y0 = min(int(floorf(ys)), H - 1);
   const int x1 = min(x0 + 1, W - 1), y1 = min(y0 + 1, H - 1);
-  tp.i00 = y0 * W + x0, tp.i01 = y0 * W + x1, tp.i10 = y1 * W + x0, tp.i11 = y1 * W + x1;
+  tp.x0 = x0, tp.x1 = x1, tp.y0 = y0, tp.y1 = y1;
   tp.fx = __fsub_rn(xs, float(x0)), tp.fy = __fsub_rn(ys, float(y0));
   return true;
 }
@@ -1257,8 +1257,33 @@ __global__ void k_warp(const float *__restrict__ src, float *__restrict__ dst, i
   if (warp_sample(src, W, H, c, int(t % W), int(t / W), v)) dst[t] = v;
 }
 
-// Rotates every per-angle image, masks and sums over angles in FP64, and
-// averages (src/cudaMain.cu:830-909, include/uniaxial.h:958-992).
+// Angle sums in float-float arithmetic: Knuth's TwoSum keeps hi + lo equal to
+// the running sum of the FP32 samples to about 2^-48 relative, so the final
+// float(sum / n) agrees with the reference's FP64 accumulation
+// (src/cudaMain.cu:887-905) except where the exact mean lies within ~1e-13 of
+// a rounding boundary.  The FP32 pipe does it; GB300's FP64 pipe is 1/64 rate.
+struct AngleSum {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float s = __fadd_rn(hi, v);
+    const float bp = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(v, bp));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+  }
+  __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+};
+
+// Mean over the angles as the reference forms it: with the rotation mask, NaN
+// samples are skipped and counted out (0 when none is left); without it a
+// NaN sample makes the mean NaN.
+__device__ __forceinline__ float angle_mean(const AngleSum &s, uint32_t count, uint32_t nangles, uint32_t rot_mask) {
+  if (rot_mask) return count == 0 ? 0.f : float(s.value() / double(count));
+  return float(s.value() / double(nangles));
+}
+
+// Rotates every per-angle image, masks and sums over angles, and averages
+// (src/cudaMain.cu:830-909, include/uniaxial.h:958-992).
 struct RotateParams {
   const float *images;      // [batch = blockIdx.y][nangles][P]
   const WarpCoef *coef;     // [nangles]
@@ -1274,111 +1299,150 @@ __global__ void __launch_bounds__(256) k_rotate_average(RotateParams p) {
   if (t >= npix) return;
   const int xd = int(t % p.W), yd = int(t / p.W);
   const float *images = p.images + size_t(blockIdx.y) * p.nangles * npix;
-  double sum = 0.0;
+  AngleSum sum;
   uint32_t count = 0;
   for (uint32_t a = 0; a < p.nangles; ++a) {
     float v = __int_as_float(0x7fc00000);
     warp_sample(images + size_t(a) * npix, p.W, p.H, p.coef[a], xd, yd, v);
     if (p.rot_mask) {
-      if (isnan(v)) {
-        v = 0.f;
-      } else {
-        ++count;
-      }
+      if (isnan(v)) continue;
+      ++count;
     }
-    sum += double(v);
+    sum.add(v);
   }
-  float r;
-  if (p.rot_mask) {
-    r = count == 0 ? 0.f : float(sum / double(count));
-  } else {
-    r = float(sum / double(p.nangles));
-  }
-  p.avg[size_t(blockIdx.y) * npix + t] = r;
+  p.avg[size_t(blockIdx.y) * npix + t] = angle_mean(sum, count, p.nangles, p.rot_mask);
+}
+
+// Gram records: the Gram matrices of NEP energies of one pixel, energy s at
+// float s * NG, padded to whole float4s.  NEP = 1 is the per-energy layout
+// (GramLayout); the field-spectrum path packs 12 floats per record (4
+// energies at NB = 2, 2 at NB = 3), so no load fetches padding.
+template <int NB, int NEP>
+struct GramRec {
+  static constexpr int NG = NB * (NB + 1) / 2;
+  static constexpr int RQ = (NEP * NG + 3) / 4;  // float4 per pixel
+};
+
+template <int NB>
+__host__ __device__ constexpr int packed_energies() {
+  return 12 / (NB * (NB + 1) / 2);
 }
 
 // Rotation and angle average from Gram maps (LAB frame): per angle a the
 // corners' Gram matrices are blended as NPP blends intensities, then
 // I(a) = sum_{b,b'} E_b(a) E_b'(a) G_bb' (the blend is linear, so this equals
-// blending the per-angle intensities).  Accumulation in FP64 as in
-// k_rotate_average.  The loads of kRotUnroll angles are issued together
-// (out-of-image angles read pixel 0 and are discarded).
+// blending the per-angle intensities).  One thread forms one destination
+// pixel for the NEP energies of its record group, so the tap arithmetic and
+// each corner load serve all of them.  A NaN at any corner makes the blend
+// NaN, so a tap with a corner outside its row's possibly-valid column range
+// (the union over the group's energies of rows[e][y] = [x, y], conservative:
+// every pixel outside is NaN) is a NaN sample without a load.
 struct RotateGramParams {
-  const float4 *gram;       // [batch = blockIdx.y][P][NQ]
+  const float4 *gram;       // [group = blockIdx.y][P][RQ]
   const WarpCoef *coef;     // [nangles]
   const float *ecoef;       // [nangles][NB]
+  const int2 *rows;         // [energy][H] from the launch's first energy, or null: no bound known
   int W, H;
   uint32_t nangles;
+  uint32_t nenergies;       // energies of this launch (the last group may be partial)
   uint32_t rot_mask;
-  float *avg;               // [batch][P]
+  float *avg;               // [energy][P]
 };
-
-constexpr int kRotUnroll = 4;
 
 // Blocks own 16 x 16 destination tiles (a warp: 16 x 2), so the rotated
 // source taps of a warp stay within a few cache lines.
 constexpr int kRotTile = 16;
 
-template <int NB>
-__global__ void __launch_bounds__(kRotTile * kRotTile) k_rotate_gram(RotateGramParams p) {
-  constexpr int NQ = GramLayout<NB>::NQ, NG = GramLayout<NB>::NG;
+template <int NB, int NEP>
+__global__ void __launch_bounds__(kRotTile * kRotTile, 2) k_rotate_gram(RotateGramParams p) {
+  constexpr int NG = GramRec<NB, NEP>::NG, RQ = GramRec<NB, NEP>::RQ;
+  constexpr int U = RQ == 1 ? 4 : RQ == 2 ? 2 : 1;  // angles whose loads are issued together
+  extern __shared__ int2 rows[];                    // [H] when p.rows is set
+  const uint32_t group = blockIdx.y;
+  const int ne = int(min(uint32_t(NEP), p.nenergies - group * NEP));
+  if (p.rows)
+    for (int y = int(threadIdx.x); y < p.H; y += int(blockDim.x)) {
+      int2 r = p.rows[size_t(group) * NEP * p.H + y];
+      for (int s = 1; s < ne; ++s) {
+        const int2 q = p.rows[(size_t(group) * NEP + s) * p.H + y];
+        r.x = min(r.x, q.x), r.y = max(r.y, q.y);
+      }
+      rows[y] = r;
+    }
+  __syncthreads();
   const size_t npix = size_t(p.W) * p.H;
   const int tiles_x = (p.W + kRotTile - 1) / kRotTile;
   const int xd = int(blockIdx.x % tiles_x) * kRotTile + int(threadIdx.x % kRotTile);
   const int yd = int(blockIdx.x / tiles_x) * kRotTile + int(threadIdx.x / kRotTile);
   if (xd >= p.W || yd >= p.H) return;
-  const size_t t = size_t(yd) * p.W + xd;
-  const float4 *gm = p.gram + size_t(blockIdx.y) * npix * NQ;
-  double sum = 0.0;
-  uint32_t count = 0;
-  for (uint32_t a0 = 0; a0 < p.nangles; a0 += kRotUnroll) {
-    WarpTap tp[kRotUnroll];
-    bool in[kRotUnroll];
-    float4 cv[kRotUnroll][4][NQ];
+  const float4 *gm = p.gram + size_t(group) * npix * RQ;
+  AngleSum sum[NEP];
+  uint32_t count[NEP];
 #pragma unroll
-    for (int u = 0; u < kRotUnroll; ++u) {
+  for (int s = 0; s < NEP; ++s) count[s] = 0;
+  for (uint32_t a0 = 0; a0 < p.nangles; a0 += U) {
+    WarpTap tp[U];
+    bool in[U];
+    float4 cv[U][4][RQ];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
       const uint32_t a = a0 + u;
       in[u] = a < p.nangles && warp_tap(p.W, p.H, p.coef[a < p.nangles ? a : 0], xd, yd, tp[u]);
-      if (!in[u]) tp[u] = WarpTap{0, 0, 0, 0, 0.f, 0.f};
-      const int idx[4] = {tp[u].i00, tp[u].i01, tp[u].i10, tp[u].i11};
+      if (in[u] && p.rows) {
+        const int2 r0 = rows[tp[u].y0], r1 = rows[tp[u].y1];
+        in[u] = tp[u].x0 >= r0.x && tp[u].x1 <= r0.y && tp[u].x0 >= r1.x && tp[u].x1 <= r1.y;
+      }
+      if (in[u]) {
+        const int idx[4] = {tp[u].y0 * p.W + tp[u].x0, tp[u].y0 * p.W + tp[u].x1, tp[u].y1 * p.W + tp[u].x0,
+                            tp[u].y1 * p.W + tp[u].x1};
 #pragma unroll
-      for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < 4; ++c)
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) cv[u][c][q] = __ldg(&gm[size_t(idx[c]) * NQ + q]);
+          for (int q = 0; q < RQ; ++q) cv[u][c][q] = __ldg(&gm[size_t(idx[c]) * RQ + q]);
+      }
     }
 #pragma unroll
-    for (int u = 0; u < kRotUnroll; ++u) {
+    for (int u = 0; u < U; ++u) {
       const uint32_t a = a0 + u;
       if (a >= p.nangles) break;
-      float v = __int_as_float(0x7fc00000);
-      if (in[u]) {
-        float G[NG];
+      // per-angle weights of the Gram entries: E_b E_b' (x2 off the diagonal)
+      float wq[NG];
+      {
+        float e[NB];
 #pragma unroll
-        for (int g = 0; g < NG; ++g) {
-          const int q = g / 4, r = g % 4;
-          auto comp = [&](const float4 &f) { return r == 0 ? f.x : r == 1 ? f.y : r == 2 ? f.z : f.w; };
-          G[g] = warp_blend(tp[u].fx, tp[u].fy, comp(cv[u][0][q]), comp(cv[u][1][q]), comp(cv[u][2][q]),
-                            comp(cv[u][3][q]));
-        }
-        v = gram_intensity<NB>(G, p.ecoef + size_t(a) * NB);
+        for (int b = 0; b < NB; ++b) e[b] = __ldg(&p.ecoef[size_t(a) * NB + b]);
+        int q = 0;
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+          for (int b2 = b; b2 < NB; ++b2) wq[q++] = (b == b2 ? 1.f : 2.f) * e[b] * e[b2];
       }
-      if (p.rot_mask) {
-        if (isnan(v)) {
+#pragma unroll
+      for (int s = 0; s < NEP; ++s) {
+        if (s >= ne) break;
+        float v = __int_as_float(0x7fc00000);
+        if (in[u]) {
           v = 0.f;
-        } else {
-          ++count;
+#pragma unroll
+          for (int g = 0; g < NG; ++g) {
+            const int f = s * NG + g, q = f / 4, r = f % 4;
+            auto comp = [&](const float4 &x) { return r == 0 ? x.x : r == 1 ? x.y : r == 2 ? x.z : x.w; };
+            const float G = warp_blend(tp[u].fx, tp[u].fy, comp(cv[u][0][q]), comp(cv[u][1][q]),
+                                       comp(cv[u][2][q]), comp(cv[u][3][q]));
+            v += wq[g] * G;
+          }
         }
+        if (p.rot_mask) {
+          if (isnan(v)) continue;
+          ++count[s];
+        }
+        sum[s].add(v);
       }
-      sum += double(v);
     }
   }
-  float r;
-  if (p.rot_mask) {
-    r = count == 0 ? 0.f : float(sum / double(count));
-  } else {
-    r = float(sum / double(p.nangles));
-  }
-  p.avg[size_t(blockIdx.y) * npix + t] = r;
+#pragma unroll
+  for (int s = 0; s < NEP; ++s)
+    if (s < ne) p.avg[(size_t(group) * NEP + s) * npix + size_t(yd) * p.W + xd] = angle_mean(sum[s], count[s], p.nangles, p.rot_mask);
 }
 
 __global__ void k_fill(float *dst, size_t n, float v, size_t stride = 0) {
