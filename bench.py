@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "c2", "c4", "z64", "c1", "small"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "c2", "c4", "z64", "cube256", "c1", "small"])
     ap.add_argument("--energies-per-step", type=int, default=ENERGIES_PER_STEP)
     ap.add_argument("--strategy", type=int, default=0, choices=[0, 1, 2],
                     help="0 auto, 1 per-energy spectra, 2 field spectra once per request")

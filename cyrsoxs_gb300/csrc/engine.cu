@@ -1028,10 +1028,17 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
     if (up) CYR_TRY(const_cast<SlabUpload *>(up)->issue(sl + 1));  // the next slab's copy, behind this slab's kernels
   }
   CYR_TRY(fft_axes(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st, 2, 2));
-  int slot = -1;
+  // bin 0 of each packed volume replaced by the mean of its neighbours
+  CYR_TRY(sc.dc.ensure(size_t(kMaxPacked) * sizeof(float2)));
+  int slot = ctx.prof.begin(kDc, st);
+  k_dc<<<1, (npk + 31) / 32 * 32, 0, st>>>(spec, npk, pl.nvox, pl.nx, pl.ny, pl.nz, 0, 1 % pl.nz, pl.nz - 1,
+                                           sc.dc.as<float2>());
+  ctx.prof.end(slot, st);
+  CYR_CUDA(cudaGetLastError());
 
   FieldEwaldParams fe{};
-  fe.zspec = spec;  // every Ewald block forms the DC replacement of each packed volume
+  fe.zspec = spec;
+  fe.zdc = sc.dc.as<float2>();
   fe.npk = npk;
   fe.nvox = pl.nvox;
   fe.coef = reinterpret_cast<const float4 *>(dp + pl.off_fcoef);

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
 // rotation R^T folded in, include/uniaxial.h:163-165).
 struct FieldEwaldParams {
   const float2 *zspec;   // [npk][nz][ny][nx], unshifted (natural) bin order
-  // the DC replacement of each packed volume is formed by every block (dc_mean)
+  const float2 *zdc;     // [npk] DC replacement of each packed volume (k_dc)
   uint32_t npk;
   size_t nvox;
   const float4 *coef;    // [ne][6][npk]: (alpha.x, alpha.y, beta.x, beta.y)
@@ -149,12 +149,9 @@ constexpr int kFieldGather = 4;  // packed volumes whose loads are issued togeth
 template <int NB>
 __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldParams p) {
   extern __shared__ float4 fcoef[];  // [6][npk]
-  __shared__ float2 zdc[kMaxPacked];
   const uint32_t eb = blockIdx.x % p.nbatch, e = p.e0 + eb;
   const uint32_t nx = p.g.nx, ny = p.g.ny, nz = p.g.nz;
   for (uint32_t t = threadIdx.x; t < 6 * p.npk; t += blockDim.x) fcoef[t] = p.coef[size_t(e) * 6 * p.npk + t];
-  for (uint32_t j = threadIdx.x; j < p.npk; j += blockDim.x)
-    zdc[j] = dc_mean(p.zspec + size_t(j) * p.nvox, nx, ny, nz, 0, 1 % nz, nz - 1);
   __syncthreads();
   const size_t npix = size_t(nx) * ny;
   const size_t t = size_t(blockIdx.x / p.nbatch) * blockDim.x + threadIdx.x;
@@ -184,69 +181,82 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   const uint32_t ux = igor(X, nx), uy = igor(Y, ny);
   const uint32_t mx = ux ? nx - ux : 0u, my = uy ? ny - uy : 0u;
   const float d = g.kmag * g.kmag;
-  constexpr int NG = NB > 0 ? NB * (NB + 1) / 2 : 1;
-  float G[NG] = {};
-  float2 Nk[NB > 0 ? 1 : 2][6];  // NB = 0 keeps both planes' entries for the angle loop
-  float Q[2][3];
-  for (int pl = 0; pl < nplanes; ++pl) {
-    const uint32_t uz = g.twod ? 0u : igor(zs[pl], nz);
+  // Z_j(k) and Z_j(-k) at both planes: the loads of kFieldGather volumes of
+  // both planes are issued together, and each coefficient serves both planes
+  size_t i0[2], i1[2];
+  bool is_dc[2];
+#pragma unroll
+  for (int pl = 0; pl < 2; ++pl) {
+    const uint32_t uz = (g.twod || pl >= nplanes) ? 0u : igor(zs[pl], nz);
     const uint32_t mz = uz ? nz - uz : 0u;
-    const bool is_dc = ux == 0 && uy == 0 && uz == 0;
-    const size_t i0 = size_t(ux) + size_t(uy) * nx + size_t(uz) * npix;
-    const size_t i1 = size_t(mx) + size_t(my) * nx + size_t(mz) * npix;
-    float2 N[6];
+    is_dc[pl] = ux == 0 && uy == 0 && uz == 0;
+    i0[pl] = size_t(ux) + size_t(uy) * nx + size_t(uz) * npix;
+    i1[pl] = size_t(mx) + size_t(my) * nx + size_t(mz) * npix;
+  }
+  const bool two = nplanes == 2;
+  float2 N[2][6];
 #pragma unroll
-    for (int v = 0; v < 6; ++v) N[v] = make_float2(0.f, 0.f);
-    for (uint32_t j0 = 0; j0 < p.npk; j0 += kFieldGather) {
-      float2 za[kFieldGather], zb[kFieldGather];
+  for (int pl = 0; pl < 2; ++pl)
 #pragma unroll
-      for (int q = 0; q < kFieldGather; ++q) {
-        const uint32_t j = j0 + q;
-        za[q] = zb[q] = make_float2(0.f, 0.f);
-        if (j < p.npk) {
-          if (is_dc) {
-            za[q] = zb[q] = zdc[j];
+    for (int v = 0; v < 6; ++v) N[pl][v] = make_float2(0.f, 0.f);
+  for (uint32_t j0 = 0; j0 < p.npk; j0 += kFieldGather) {
+    float2 za[2][kFieldGather], zb[2][kFieldGather];
+#pragma unroll
+    for (int q = 0; q < kFieldGather; ++q) {
+      const uint32_t j = j0 + q;
+#pragma unroll
+      for (int pl = 0; pl < 2; ++pl) {
+        za[pl][q] = zb[pl][q] = make_float2(0.f, 0.f);
+        if (j < p.npk && (pl == 0 || two)) {
+          if (is_dc[pl]) {
+            za[pl][q] = zb[pl][q] = p.zdc[j];
           } else {
             const float2 *zj = p.zspec + size_t(j) * p.nvox;
-            za[q] = __ldg(&zj[i0]);
-            zb[q] = __ldg(&zj[i1]);
+            za[pl][q] = __ldg(&zj[i0[pl]]);
+            zb[pl][q] = __ldg(&zj[i1[pl]]);
           }
         }
       }
+    }
 #pragma unroll
-      for (int q = 0; q < kFieldGather; ++q) {
-        const uint32_t j = j0 + q;
-        if (j >= p.npk) break;
-        const float2 a = za[q], b = make_float2(zb[q].x, -zb[q].y);  // b = conj Z_j(-k)
+    for (int q = 0; q < kFieldGather; ++q) {
+      const uint32_t j = j0 + q;
+      if (j >= p.npk) break;
 #pragma unroll
-        for (int v = 0; v < 6; ++v) {
-          const float4 c = fcoef[v * p.npk + j];
-          N[v].x += c.x * a.x - c.y * a.y + c.z * b.x - c.w * b.y;
-          N[v].y += c.x * a.y + c.y * a.x + c.z * b.y + c.w * b.x;
+      for (int v = 0; v < 6; ++v) {
+        const float4 c = fcoef[v * p.npk + j];
+#pragma unroll
+        for (int pl = 0; pl < 2; ++pl) {
+          const float2 a = za[pl][q], b = make_float2(zb[pl][q].x, -zb[pl][q].y);  // b = conj Z_j(-k)
+          N[pl][v].x += c.x * a.x - c.y * a.y + c.z * b.x - c.w * b.y;
+          N[pl][v].y += c.x * a.y + c.y * a.x + c.z * b.y + c.w * b.x;
         }
       }
     }
+  }
+  float Q[2][3];
+#pragma unroll
+  for (int pl = 0; pl < 2; ++pl) {
     Q[pl][0] = g.kx + p.qx[X];
     Q[pl][1] = g.ky + p.qy[Y];
-    Q[pl][2] = g.kz + (g.twod ? 0.f : p.qz[zs[pl]]);
-    if constexpr (NB > 0) {
+    Q[pl][2] = g.kz + ((g.twod || pl >= nplanes) ? 0.f : p.qz[zs[pl]]);
+  }
+  if constexpr (NB > 0) {
+    constexpr int NG = NB * (NB + 1) / 2;
+    float G[NG] = {};
+    for (int pl = 0; pl < nplanes; ++pl) {
       // symmetric entry (c, b) of Nt: volumes xx xy xz yy yz zz
       float2 P[3][NB];
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
-        P[0][b] = N[b == 0 ? 0 : b == 1 ? 1 : 2];
-        P[1][b] = N[b == 0 ? 1 : b == 1 ? 3 : 4];
-        P[2][b] = N[b == 0 ? 2 : b == 1 ? 4 : 5];
+        P[0][b] = N[pl][b == 0 ? 0 : b == 1 ? 1 : 2];
+        P[1][b] = N[pl][b == 0 ? 1 : b == 1 ? 3 : 4];
+        P[2][b] = N[pl][b == 0 ? 2 : b == 1 ? 4 : 5];
       }
-      gram_add<NB>(Q[pl], d, P, nplanes == 2 ? (pl == 0 ? 1.f - w1 : w1) : 1.f, G);
-    } else {
-#pragma unroll
-      for (int v = 0; v < 6; ++v) Nk[pl][v] = N[v];
+      gram_add<NB>(Q[pl], d, P, two ? (pl == 0 ? 1.f - w1 : w1) : 1.f, G);
     }
-  }
-  if constexpr (NB > 0) {
 #pragma unroll
-    for (int q = 0; q < NGG; ++q) gm[q] = G[q];
+    for (int q = 0; q < NG; ++q) gm[q] = G[q];
   } else {
     const float w0 = 1.f - w1;
     for (uint32_t a = 0; a < p.nangles; ++a) {
@@ -258,12 +268,12 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
         for (int c = 0; c < 3; ++c) {
           float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-          for (int v = 0; v < 6; ++v) acc = cfma(__ldg(&M[c * 6 + v]), Nk[pl][v], acc);
+          for (int v = 0; v < 6; ++v) acc = cfma(__ldg(&M[c * 6 + v]), N[pl][v], acc);
           pc[c] = acc;
         }
         I[pl] = intensity(Q[pl][0], Q[pl][1], Q[pl][2], d, pc[0], pc[1], pc[2]);
       }
-      img[size_t(a) * npix] = nplanes == 2 ? w0 * I[0] + w1 * I[1] : I[0];
+      img[size_t(a) * npix] = two ? w0 * I[0] + w1 * I[1] : I[0];
     }
   }
 }

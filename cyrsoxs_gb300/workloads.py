@@ -66,6 +66,9 @@ def workload(name: str, energies=None) -> Workload:
     if name == "z64":  # the c2 physics on a 64 x 512 x 512 grid: a profiling size (about 3.5 GB on the device)
         es = energies or [float(e) for e in np.linspace(270.0, 300.0, 50)]
         return Workload("z64", 64, 512, 512, 4, es, (0.0, 175.0, 5.0), 2.0, 2, "random")
+    if name == "cube256":  # the headline physics on a 256^3 grid: a profiling size (about 3 GB on the device)
+        es = energies or [float(e) for e in np.linspace(270.0, 300.0, 50)]
+        return Workload("cube256", 256, 256, 256, 4, es, (0.0, 175.0, 5.0), 2.0, 5, "random")
     if name == "c4":  # large precision study: 3 materials on 256 x 1024 x 1024, 10 energies x 24 E angles
         es = energies or [float(e) for e in np.linspace(270.0, 300.0, 10)]
         return Workload("c4", 256, 1024, 1024, 3, es, (0.0, 172.5, 7.5), 2.0, 4, "random")
