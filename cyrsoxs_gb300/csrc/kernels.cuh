@@ -565,6 +565,10 @@ __host__ __device__ constexpr uint32_t swz_mask(uint32_t h) {  // h = p >> 4
          ((h & 16u) ? 12u : 0u);
 }
 __device__ __forceinline__ uint32_t swz(uint32_t p) { return p ^ swz_mask(p >> 4); }
+// swz(t + 32 i) for t < 32 given tx = swz(t): swz_mask is linear over GF(2)
+// and t, 32 i occupy disjoint bits, so swz(t | 32 i) = swz(t) ^ 32 i ^
+// swz_mask(2 i); with i a compile-time constant that is a single XOR.
+__device__ __forceinline__ uint32_t swz_at(uint32_t tx, uint32_t i) { return tx ^ (32u * i) ^ swz_mask(2u * i); }
 // Stride between the lines of TX interleaved columns: congruent to 16 / TX
 // (1 for TX >= 16) modulo 16, so a half-warp touching TX columns x (16 / TX)
 // consecutive positions hits 16 distinct 8-byte banks.
@@ -642,8 +646,9 @@ __device__ __forceinline__ void warp_stage(float2 (&v)[V], float2 *line, const f
   }
   if (!LAST) {
     __syncwarp();
+    const uint32_t lx = swz(lane);
 #pragma unroll
-    for (int i = 0; i < V; ++i) v[i] = line[swz(lane + 32 * i)];
+    for (int i = 0; i < V; ++i) v[i] = line[V >= 16 ? swz_at(lx, i) : swz(lane + 32 * i)];
     __syncwarp();
   }
 }
@@ -706,8 +711,12 @@ struct ColPassParams {
   const float2 *tw;
 };
 
+// Blocks per SM the register budget is set for: 32 registers a thread up to
+// 256-point lines, 64 for 512, 128 for 1024.
+__host__ __device__ constexpr int cols_min_blocks(int v, int tx) { return (v <= 8 ? 2048 : v == 16 ? 1024 : 512) / (tx * 32); }
+
 template <int V, int TX>
-__global__ void __launch_bounds__(TX * 32) k_fft_cols(ColPassParams p) {
+__global__ void __launch_bounds__(TX * 32, cols_min_blocks(V, TX)) k_fft_cols(ColPassParams p) {
   constexpr uint32_t N = 32 * V, L = line_stride(N, TX), NT = TX * 32;
   extern __shared__ float2 smem[];
   float2 *tws = smem, *tile = smem + N;
@@ -718,31 +727,57 @@ __global__ void __launch_bounds__(TX * 32) k_fft_cols(ColPassParams p) {
   float2 *g = p.data + size_t(blockIdx.y) * p.vstride + size_t(other) * p.ostride + x0;
   const uint32_t l = threadIdx.x % TX, i0 = threadIdx.x / TX;  // compile-time TX: shifts
   constexpr uint32_t ISTEP = NT / TX;
+  static_assert(ISTEP == 32 && N / ISTEP == V, "tile rows are i0 + 32 k");
+  const uint32_t ix = swz(i0);
+  const size_t s32 = size_t(32) * p.estride;
+  float2 *gl = g + l + size_t(i0) * p.estride;
+  float2 *tl = tile + l * L;
+  // rows i0 + 32 (k0 + u), u < 4: swz_at(ix, k0 + u) = swz_at(ix, k0) ^ 32 u ^ swz_mask(2 u).
+  // (Lines of up to 256 points measured faster with the plain swizzle, here
+  // and in the warp FFT's exchanges.)
   if (l < valid) {
+    if constexpr (V >= 16) {
+      for (int k0 = 0; k0 < V; k0 += 4) {
+        const uint32_t t0 = swz_at(ix, k0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) cp_async8(&tl[t0 ^ (32u * u) ^ swz_mask(2u * u)], gl + (k0 + u) * s32);
+      }
+    } else {
 #pragma unroll 4
-    for (uint32_t i = i0; i < N; i += ISTEP) cp_async8(&tile[l * L + swz(i)], &g[l + i * p.estride]);
+      for (uint32_t i = i0; i < N; i += ISTEP) cp_async8(&tile[l * L + swz(i)], &g[l + i * p.estride]);
+    }
   } else {
-    for (uint32_t i = i0; i < N; i += ISTEP) tile[l * L + swz(i)] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < V; ++k) tl[swz_at(ix, k)] = make_float2(0.f, 0.f);
   }
   warp_twiddles<V>(tws, p.tw);
   cp_async_wait_all();
   __syncthreads();
   float2 *line = tile + warp * L;  // one warp per column
+  const uint32_t lx = swz(lane);
   float2 v[V];
 #pragma unroll
-  for (int i = 0; i < V; ++i) v[i] = line[swz(lane + 32 * i)];
+  for (int i = 0; i < V; ++i) v[i] = line[V >= 16 ? swz_at(lx, i) : swz(lane + 32 * i)];
   __syncwarp();
   warp_fft<V>(v, line, tws, lane);
 #pragma unroll
-  for (int i = 0; i < V; ++i) line[swz(lane + 32 * i)] = v[i];
+  for (int i = 0; i < V; ++i) line[V >= 16 ? swz_at(lx, i) : swz(lane + 32 * i)] = v[i];
   __syncthreads();
   if (l < valid) {
+    if constexpr (V >= 16) {
+      for (int k0 = 0; k0 < V; k0 += 4) {
+        const uint32_t t0 = swz_at(ix, k0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) gl[(k0 + u) * s32] = tl[t0 ^ (32u * u) ^ swz_mask(2u * u)];
+      }
+    } else {
 #pragma unroll 4
-    for (uint32_t i = i0; i < N; i += ISTEP) g[l + i * p.estride] = tile[l * L + swz(i)];
+      for (uint32_t i = i0; i < N; i += ISTEP) g[l + i * p.estride] = tile[l * L + swz(i)];
+    }
   }
 }
 
-// Warp-FFT form of k_build_fft_z// Per-thread register FFT for short strided lines (N = 8..64, powers of two):
+// Per-thread register FFT for short strided lines (N = 8..64, powers of two):
 // one thread owns one y or z line, and consecutive threads take consecutive
 // x, so each of a warp's N loads and N stores is one contiguous 256-byte
 // segment and no shared memory is involved.  Radix-2 decimation in
@@ -916,13 +951,14 @@ __global__ void __launch_bounds__(256) k_build_fft_z_warp(BuildZParams p, const 
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (uint32_t li = warp; li < nvol * TX; li += nwarps) {
     float2 *line = lines + li * L;
+    const uint32_t lx = swz(lane);
     float2 v[V];
 #pragma unroll
-    for (int i = 0; i < V; ++i) v[i] = line[swz(lane + 32 * i)];
+    for (int i = 0; i < V; ++i) v[i] = line[swz_at(lx, i)];
     __syncwarp();
     warp_fft<V>(v, line, tws, lane);
 #pragma unroll
-    for (int i = 0; i < V; ++i) line[swz(lane + 32 * i)] = v[i];
+    for (int i = 0; i < V; ++i) line[swz_at(lx, i)] = v[i];
     __syncwarp();
   }
   __syncthreads();
