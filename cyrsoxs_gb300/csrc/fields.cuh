@@ -134,7 +134,7 @@ struct FieldEwaldParams {
   const float *mat;      // NB = 0: [nangles][3][6]
   const float *ecoef;    // NB > 0: [nangles][NB] E components of the LAB angle basis
   float *images;         // NB = 0: [batch][nangles][npix]
-  float4 *gram;          // NB > 0: Gram records [batch / NEP][npix][RQ] (GramRec<NB, packed_energies<NB>()>)
+  float4 *gram;          // NB > 0: Gram records [batch / NEP][RQ][npix] (GramRec<NB, packed_energies<NB>()>)
   uint32_t nbatch;       // energies of this launch
 };
 
@@ -165,13 +165,15 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   int nplanes;
   float *img = p.images + size_t(eb) * p.nangles * npix + t;
   constexpr int NBG = NB > 0 ? NB : 1, NEP = packed_energies<NBG>();
-  constexpr int NGG = GramRec<NBG, NEP>::NG;
-  float *gm = reinterpret_cast<float *>(p.gram + (size_t(eb / NEP) * npix + t) * GramRec<NBG, NEP>::RQ) +
-              (eb % NEP) * NGG;
+  constexpr int NGG = GramRec<NBG, NEP>::NG, RQ = GramRec<NBG, NEP>::RQ;
+  // component g of this energy: float f = (eb % NEP) NGG + g of the record, plane f / 4, lane f % 4
+  float *gm = reinterpret_cast<float *>(p.gram + size_t(eb / NEP) * RQ * npix + t);
+  const uint32_t f0 = (eb % NEP) * NGG;
+  auto gput = [&](int g, float v) { gm[size_t((f0 + g) / 4) * npix * 4 + (f0 + g) % 4] = v; };
   if (!ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes)) {
     if constexpr (NB > 0) {
 #pragma unroll
-      for (int q = 0; q < NGG; ++q) gm[q] = __int_as_float(0x7fc00000);
+      for (int q = 0; q < NGG; ++q) gput(q, __int_as_float(0x7fc00000));
     } else {
       const float nanv = __int_as_float(0x7fc00000);
       for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
       gram_add<NB>(Q[pl], d, P, two ? (pl == 0 ? 1.f - w1 : w1) : 1.f, G);
     }
 #pragma unroll
-    for (int q = 0; q < NG; ++q) gm[q] = G[q];
+    for (int q = 0; q < NG; ++q) gput(q, G[q]);
   } else {
     const float w0 = 1.f - w1;
     for (uint32_t a = 0; a < p.nangles; ++a) {

@@ -1027,7 +1027,7 @@ struct EwaldParams {
   uint32_t zlo, nplanes;
   unsigned int *errors;   // incremented when a needed plane is not stored
   uint32_t nbasis;        // 1..3
-  float4 *gram;           // when set: Gram maps [P][NQ] instead of per-angle images
+  float4 *gram;           // when set: Gram maps [NQ][P] instead of per-angle images
   uint32_t vol[3][3];     // vol[c][b]: volume holding component c of basis b
   uint32_t nangles;
   const float *coef;      // [nangles][nbasis]
@@ -1091,7 +1091,7 @@ __device__ __forceinline__ float gram_intensity(const float (&G)[NB * (NB + 1) /
   return I;
 }
 
-// Gram maps: NB = 1 or 2 -> one float4 per pixel (G00 [G01 G11]), NB = 3 -> two
+// Gram maps: NB = 1 or 2 -> one float4 plane (G00 [G01 G11]), NB = 3 -> two
 // (G00 G01 G02 G11 | G12 G22); a NaN pixel stores NaN in every component.
 template <int NB>
 struct GramLayout {
@@ -1099,21 +1099,22 @@ struct GramLayout {
   static constexpr int NQ = (NG + 3) / 4;
 };
 
+// gm: the pixel's float4 in plane 0; plane q at gm + q * plane.
 template <int NB>
-__device__ __forceinline__ void gram_store(float4 *gm, const float (&G)[NB * (NB + 1) / 2]) {
+__device__ __forceinline__ void gram_store(float4 *gm, size_t plane, const float (&G)[NB * (NB + 1) / 2]) {
   constexpr int NG = GramLayout<NB>::NG, NQ = GramLayout<NB>::NQ;
   float v[4 * NQ];
 #pragma unroll
   for (int q = 0; q < 4 * NQ; ++q) v[q] = q < NG ? G[q] : 0.f;
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) gm[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  for (int q = 0; q < NQ; ++q) gm[q * plane] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
 }
 
 template <int NB>
-__device__ __forceinline__ void gram_store_nan(float4 *gm) {
+__device__ __forceinline__ void gram_store_nan(float4 *gm, size_t plane) {
   const float n = __int_as_float(0x7fc00000);
 #pragma unroll
-  for (int q = 0; q < GramLayout<NB>::NQ; ++q) gm[q] = make_float4(n, n, n, n);
+  for (int q = 0; q < GramLayout<NB>::NQ; ++q) gm[q * plane] = make_float4(n, n, n, n);
 }
 
 __device__ __forceinline__ float intensity(float Q0, float Q1, float Q2, float d, float2 p0, float2 p1, float2 p2) {
@@ -1179,10 +1180,10 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
   const bool isnan_px = !ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes);
   const float nanv = __int_as_float(0x7fc00000);
   float *img = p.images + t;
-  float4 *gm = p.gram ? p.gram + t * GramLayout<NB>::NQ : nullptr;
+  float4 *gm = p.gram ? p.gram + t : nullptr;  // planes of npix float4
   if (isnan_px) {
     if (gm) {
-      gram_store_nan<NB>(gm);
+      gram_store_nan<NB>(gm, npix);
       return;
     }
     for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
@@ -1200,7 +1201,7 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
       if (zs[pl] < p.zlo || pz >= p.nplanes) {  // the host's plane range missed this pixel
         atomicAdd(p.errors, 1u);
         if (gm) {
-          gram_store_nan<NB>(gm);
+          gram_store_nan<NB>(gm, npix);
           return;
         }
         for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
@@ -1221,7 +1222,7 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
     gram_add<NB>(Q, d, P, nplanes == 2 ? (pl == 0 ? 1.f - w1 : w1) : 1.f, G);
   }
   if (gm) {
-    gram_store<NB>(gm, G);
+    gram_store<NB>(gm, npix, G);
     return;
   }
   for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = gram_intensity<NB>(G, p.coef + size_t(a) * NB);
@@ -1350,9 +1351,11 @@ __global__ void __launch_bounds__(256) k_rotate_average(RotateParams p) {
 }
 
 // Gram records: the Gram matrices of NEP energies of one pixel, energy s at
-// float s * NG, padded to whole float4s.  NEP = 1 is the per-energy layout
-// (GramLayout); the field-spectrum path packs 12 floats per record (4
-// energies at NB = 2, 2 at NB = 3), so no load fetches padding.
+// float s * NG, padded to whole float4s and stored as RQ planes of float4
+// ([group][RQ][pixel]), so each of a warp's loads reads whole 16-byte pixels
+// of one plane.  NEP = 1 is the per-energy layout (GramLayout); the
+// field-spectrum path packs 12 floats per record (4 energies at NB = 2, 2 at
+// NB = 3), so no load fetches padding.
 template <int NB, int NEP>
 struct GramRec {
   static constexpr int NG = NB * (NB + 1) / 2;
@@ -1374,7 +1377,7 @@ __host__ __device__ constexpr int packed_energies() {
 // (the union over the group's energies of rows[e][y] = [x, y], conservative:
 // every pixel outside is NaN) is a NaN sample without a load.
 struct RotateGramParams {
-  const float4 *gram;       // [group = blockIdx.y][P][RQ]
+  const float4 *gram;       // [group = blockIdx.y][RQ][P]
   const WarpCoef *coef;     // [nangles]
   const float *ecoef;       // [nangles][NB]
   const int2 *rows;         // [energy][H] from the launch's first energy, or null: no bound known
@@ -1390,7 +1393,7 @@ struct RotateGramParams {
 constexpr int kRotTile = 16;
 
 template <int NB, int NEP>
-__global__ void __launch_bounds__(kRotTile * kRotTile, 2) k_rotate_gram(RotateGramParams p) {
+__global__ void __launch_bounds__(kRotTile * kRotTile, 3) k_rotate_gram(RotateGramParams p) {
   constexpr int NG = GramRec<NB, NEP>::NG, RQ = GramRec<NB, NEP>::RQ;
   constexpr int U = RQ == 1 ? 4 : RQ == 2 ? 2 : 1;  // angles whose loads are issued together
   extern __shared__ int2 rows[];                    // [H] when p.rows is set
@@ -1434,7 +1437,7 @@ __global__ void __launch_bounds__(kRotTile * kRotTile, 2) k_rotate_gram(RotateGr
 #pragma unroll
         for (int c = 0; c < 4; ++c)
 #pragma unroll
-          for (int q = 0; q < RQ; ++q) cv[u][c][q] = __ldg(&gm[size_t(idx[c]) * RQ + q]);
+          for (int q = 0; q < RQ; ++q) cv[u][c][q] = __ldg(&gm[q * npix + idx[c]]);
       }
     }
 #pragma unroll
