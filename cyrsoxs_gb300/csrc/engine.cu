@@ -496,7 +496,7 @@ size_t image_bytes(const Plan &pl, uint32_t nb = 1) {
   if (pl.material_frame) return size_t(nb) * pl.nang * pl.npix * sizeof(float);
   const uint32_t nep = gram_nep(pl), ng = pl.nbasis * (pl.nbasis + 1) / 2;
   const size_t rq = (size_t(nep) * ng + 3) / 4;
-  return size_t((nb + nep - 1) / nep) * pl.npix * rq * sizeof(float4);
+  return size_t((nb + nep - 1) / nep) * gram_plane_size(int(pl.ny), int(pl.nx)) * rq * sizeof(float4);
 }
 
 // Device bytes of the FIELDS strategy: packed field spectra, per-batch images and averages.
@@ -1056,6 +1056,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   fe.nangles = pl.nang;
   fe.images = sc.images.as<float>();
   fe.gram = sc.images.as<float4>();
+  fe.gplane = gram_plane_size(int(pl.ny), int(pl.nx));
   const size_t fsmem = size_t(6) * npk * sizeof(float4);
   const unsigned pix_blocks = unsigned((pl.npix + 255) / 256);
   const unsigned fpix_blocks = unsigned((pl.npix + kFieldEwaldThreads - 1) / kFieldEwaldThreads);
@@ -1079,6 +1080,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
     rp.avg = sc.avg.as<float>();
     RotateGramParams rg{};
     rg.gram = sc.images.as<float4>();
+    rg.plane = fe.gplane;
     rg.coef = rp.coef;
     rg.ecoef = fe.ecoef;
     rg.W = W, rg.H = H;
@@ -1429,6 +1431,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
         ep.coef = dcoef + size_t(k) * pl.nang * pl.nbasis;
         ep.images = images;
         ep.gram = reinterpret_cast<float4 *>(images);
+        ep.gplane = gram_plane_size(int(pl.ny), int(pl.nx));
         const int slot = ctx.prof.begin(kEwald, st);
         if (pl.nbasis == 2)
           k_ewald_angles<2><<<pix_blocks, 256, 0, st>>>(ep);
@@ -1470,6 +1473,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
       } else {
         RotateGramParams rg{};
         rg.gram = reinterpret_cast<const float4 *>(images);
+        rg.plane = gram_plane_size(int(pl.ny), int(pl.nx));
         rg.coef = dwarp + size_t(k) * pl.nang;
         rg.ecoef = dcoef + size_t(k) * pl.nang * pl.nbasis;
         rg.W = W, rg.H = H;

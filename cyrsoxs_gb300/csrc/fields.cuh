@@ -134,7 +134,8 @@ struct FieldEwaldParams {
   const float *mat;      // NB = 0: [nangles][3][6]
   const float *ecoef;    // NB > 0: [nangles][NB] E components of the LAB angle basis
   float *images;         // NB = 0: [batch][nangles][npix]
-  float4 *gram;          // NB > 0: Gram records [batch / NEP][RQ][npix] (GramRec<NB, packed_energies<NB>()>)
+  float4 *gram;          // NB > 0: Gram records [batch / NEP][RQ][gplane] (GramRec<NB, packed_energies<NB>()>, gram_at)
+  size_t gplane;         // float4 per Gram plane (gram_plane_size(ny, nx))
   uint32_t nbatch;       // energies of this launch
 };
 
@@ -167,9 +168,11 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   constexpr int NBG = NB > 0 ? NB : 1, NEP = packed_energies<NBG>();
   constexpr int NGG = GramRec<NBG, NEP>::NG, RQ = GramRec<NBG, NEP>::RQ;
   // component g of this energy: float f = (eb % NEP) NGG + g of the record, plane f / 4, lane f % 4
-  float *gm = reinterpret_cast<float *>(p.gram + size_t(eb / NEP) * RQ * npix + t);
+  // the rotation's image has width ny: pixel t is (x, y) = (t % ny, t / ny)
+  float *gm = reinterpret_cast<float *>(p.gram + size_t(eb / NEP) * RQ * p.gplane +
+                                        gram_at(int(t % ny), int(t / ny), int(ny)));
   const uint32_t f0 = (eb % NEP) * NGG;
-  auto gput = [&](int g, float v) { gm[size_t((f0 + g) / 4) * npix * 4 + (f0 + g) % 4] = v; };
+  auto gput = [&](int g, float v) { gm[size_t((f0 + g) / 4) * p.gplane * 4 + (f0 + g) % 4] = v; };
   if (!ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes)) {
     if constexpr (NB > 0) {
 #pragma unroll

@@ -1027,7 +1027,8 @@ struct EwaldParams {
   uint32_t zlo, nplanes;
   unsigned int *errors;   // incremented when a needed plane is not stored
   uint32_t nbasis;        // 1..3
-  float4 *gram;           // when set: Gram maps [NQ][P] instead of per-angle images
+  float4 *gram;           // when set: Gram maps [NQ][gplane] (gram_at) instead of per-angle images
+  size_t gplane;          // float4 per Gram plane (gram_plane_size(ny, nx))
   uint32_t vol[3][3];     // vol[c][b]: volume holding component c of basis b
   uint32_t nangles;
   const float *coef;      // [nangles][nbasis]
@@ -1089,6 +1090,16 @@ __device__ __forceinline__ float gram_intensity(const float (&G)[NB * (NB + 1) /
 #pragma unroll
     for (int b2 = b; b2 < NB; ++b2) I += (b == b2 ? 1.f : 2.f) * e[b] * e[b2] * G[q++];
   return I;
+}
+
+// Gram planes hold the pixels of the rotation's source image (x < W, y < H,
+// row-major index y W + x) in 4 x 2 blocks, one 128-byte line per block: the
+// rotated bilinear taps of an 8 x 4 warp tile touch about 8 lines per load,
+// where row order touches about 14.
+__host__ __device__ inline size_t gram_plane_size(int W, int H) { return size_t((H + 1) / 2) * ((W + 3) / 4) * 8; }
+__device__ __forceinline__ uint32_t gram_at(int x, int y, int W) {
+  return ((uint32_t(y) >> 1) * ((uint32_t(W) + 3) >> 2) + (uint32_t(x) >> 2)) * 8 + ((uint32_t(y) & 1) << 2) +
+         (uint32_t(x) & 3);
 }
 
 // Gram maps: NB = 1 or 2 -> one float4 plane (G00 [G01 G11]), NB = 3 -> two
@@ -1180,10 +1191,11 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
   const bool isnan_px = !ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes);
   const float nanv = __int_as_float(0x7fc00000);
   float *img = p.images + t;
-  float4 *gm = p.gram ? p.gram + t : nullptr;  // planes of npix float4
+  // the rotation's image: width ny, so pixel t is (x, y) = (t % ny, t / ny)
+  float4 *gm = p.gram ? p.gram + gram_at(int(t % p.ny), int(t / p.ny), int(p.ny)) : nullptr;
   if (isnan_px) {
     if (gm) {
-      gram_store_nan<NB>(gm, npix);
+      gram_store_nan<NB>(gm, p.gplane);
       return;
     }
     for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
@@ -1201,7 +1213,7 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
       if (zs[pl] < p.zlo || pz >= p.nplanes) {  // the host's plane range missed this pixel
         atomicAdd(p.errors, 1u);
         if (gm) {
-          gram_store_nan<NB>(gm, npix);
+          gram_store_nan<NB>(gm, p.gplane);
           return;
         }
         for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = nanv;
@@ -1222,7 +1234,7 @@ __global__ void __launch_bounds__(256) k_ewald_angles(EwaldParams p) {
     gram_add<NB>(Q, d, P, nplanes == 2 ? (pl == 0 ? 1.f - w1 : w1) : 1.f, G);
   }
   if (gm) {
-    gram_store<NB>(gm, npix, G);
+    gram_store<NB>(gm, p.gplane, G);
     return;
   }
   for (uint32_t a = 0; a < p.nangles; ++a) img[size_t(a) * npix] = gram_intensity<NB>(G, p.coef + size_t(a) * NB);
@@ -1352,8 +1364,8 @@ __global__ void __launch_bounds__(256) k_rotate_average(RotateParams p) {
 
 // Gram records: the Gram matrices of NEP energies of one pixel, energy s at
 // float s * NG, padded to whole float4s and stored as RQ planes of float4
-// ([group][RQ][pixel]), so each of a warp's loads reads whole 16-byte pixels
-// of one plane.  NEP = 1 is the per-energy layout (GramLayout); the
+// ([group][RQ][plane], pixels placed by gram_at), so each of a warp's loads
+// reads whole 16-byte pixels of one plane.  NEP = 1 is the per-energy layout (GramLayout); the
 // field-spectrum path packs 12 floats per record (4 energies at NB = 2, 2 at
 // NB = 3), so no load fetches padding.
 template <int NB, int NEP>
@@ -1377,7 +1389,8 @@ __host__ __device__ constexpr int packed_energies() {
 // (the union over the group's energies of rows[e][y] = [x, y], conservative:
 // every pixel outside is NaN) is a NaN sample without a load.
 struct RotateGramParams {
-  const float4 *gram;       // [group = blockIdx.y][RQ][P]
+  const float4 *gram;       // [group = blockIdx.y][RQ][plane] (gram_at)
+  size_t plane;             // float4 per plane (gram_plane_size(W, H))
   const WarpCoef *coef;     // [nangles]
   const float *ecoef;       // [nangles][NB]
   const int2 *rows;         // [energy][H] from the launch's first energy, or null: no bound known
@@ -1388,7 +1401,7 @@ struct RotateGramParams {
   float *avg;               // [energy][P]
 };
 
-// Blocks own 16 x 16 destination tiles (a warp: 16 x 2), so the rotated
+// Blocks own 16 x 16 destination tiles (a warp: 8 x 4), so the rotated
 // source taps of a warp stay within a few cache lines.
 constexpr int kRotTile = 16;
 
@@ -1411,10 +1424,11 @@ __global__ void __launch_bounds__(kRotTile * kRotTile, 3) k_rotate_gram(RotateGr
   __syncthreads();
   const size_t npix = size_t(p.W) * p.H;
   const int tiles_x = (p.W + kRotTile - 1) / kRotTile;
-  const int xd = int(blockIdx.x % tiles_x) * kRotTile + int(threadIdx.x % kRotTile);
-  const int yd = int(blockIdx.x / tiles_x) * kRotTile + int(threadIdx.x / kRotTile);
+  const int warp = int(threadIdx.x >> 5), lane = int(threadIdx.x & 31);
+  const int xd = int(blockIdx.x % tiles_x) * kRotTile + (warp & 1) * 8 + (lane & 7);
+  const int yd = int(blockIdx.x / tiles_x) * kRotTile + (warp >> 1) * 4 + (lane >> 3);
   if (xd >= p.W || yd >= p.H) return;
-  const float4 *gm = p.gram + size_t(group) * npix * RQ;
+  const float4 *gm = p.gram + size_t(group) * p.plane * RQ;
   AngleSum sum[NEP];
   uint32_t count[NEP];
 #pragma unroll
@@ -1432,12 +1446,12 @@ __global__ void __launch_bounds__(kRotTile * kRotTile, 3) k_rotate_gram(RotateGr
         in[u] = tp[u].x0 >= r0.x && tp[u].x1 <= r0.y && tp[u].x0 >= r1.x && tp[u].x1 <= r1.y;
       }
       if (in[u]) {
-        const int idx[4] = {tp[u].y0 * p.W + tp[u].x0, tp[u].y0 * p.W + tp[u].x1, tp[u].y1 * p.W + tp[u].x0,
-                            tp[u].y1 * p.W + tp[u].x1};
+        const uint32_t idx[4] = {gram_at(tp[u].x0, tp[u].y0, p.W), gram_at(tp[u].x1, tp[u].y0, p.W),
+                                 gram_at(tp[u].x0, tp[u].y1, p.W), gram_at(tp[u].x1, tp[u].y1, p.W)};
 #pragma unroll
         for (int c = 0; c < 4; ++c)
 #pragma unroll
-          for (int q = 0; q < RQ; ++q) cv[u][c][q] = __ldg(&gm[q * npix + idx[c]]);
+          for (int q = 0; q < RQ; ++q) cv[u][c][q] = __ldg(&gm[q * p.plane + idx[c]]);
       }
     }
 #pragma unroll
