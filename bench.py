@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--energies-per-step", type=int, default=ENERGIES_PER_STEP)
     ap.add_argument("--strategy", type=int, default=0, choices=[0, 1, 2],
                     help="0 auto, 1 per-energy spectra, 2 field spectra once per request")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-served", action="store_true", help="skip the batched and serving measurements")
     ap.add_argument("--served-only", action="store_true", help="only the batched and serving measurements")
@@ -555,6 +555,7 @@ def main():
     result["e2e"] = {"value": world * len(energies) * nang * args.e2e_steps / e2e_s, "unit": "patterns/s",
                      "h2d_bytes_per_step": int(host_vox_np.nbytes + optical.nbytes),
                      "d2h_bytes_per_step": int(host_out.nbytes), "steps": args.e2e_steps,
+                     "step_ms": [round(t * 1e3, 2) for t in e2e_times],
                      "api": "cyr_cuda_main (host buffers)"}
 
     if rank == 0 and world == 1 and not args.skip_cpu:
