@@ -954,12 +954,23 @@ struct SlabUpload {
   size_t nvox = 0, npix = 0;
   cudaStream_t stream = nullptr;
   int issue(uint32_t s) {  // queues the copies of slabs up to s
+    // planes the sample already brought (every sample_zstep-th, once it was issued) are not copied again
+    auto sampled = [&](uint32_t z) { return sample != nullptr && z % sample_zstep == 0; };
     for (; issued <= s && issued < count; ++issued) {
       const uint32_t z0 = issued * planes, z1 = std::min(nz, z0 + planes);
-      for (uint32_t m = 0; m < nmat; ++m) {
-        const size_t off = size_t(m) * nvox + size_t(z0) * npix;  // float4 elements
-        CYR_CUDA(cudaMemcpyAsync(dev + off, host + 4 * off, size_t(z1 - z0) * npix * sizeof(float4),
-                                 cudaMemcpyHostToDevice, stream));
+      for (uint32_t a = z0; a < z1;) {
+        if (sampled(a)) {
+          ++a;
+          continue;
+        }
+        uint32_t b = a + 1;
+        while (b < z1 && !sampled(b)) ++b;
+        for (uint32_t m = 0; m < nmat; ++m) {
+          const size_t off = size_t(m) * nvox + size_t(a) * npix;  // float4 elements
+          CYR_CUDA(cudaMemcpyAsync(dev + off, host + 4 * off, size_t(b - a) * npix * sizeof(float4),
+                                   cudaMemcpyHostToDevice, stream));
+        }
+        a = b;
       }
       cudaEvent_t ev = nullptr;
       CYR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
