@@ -1068,9 +1068,9 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   fe.images = sc.images.as<float>();
   fe.gram = sc.images.as<float4>();
   fe.gplane = gram_plane_size(int(pl.ny), int(pl.nx));
-  const size_t fsmem = size_t(6) * npk * sizeof(float4);
+  const size_t fsmem = size_t(kEwaldEnergies) * 6 * npk * sizeof(float4);
   const unsigned pix_blocks = unsigned((pl.npix + 255) / 256);
-  const unsigned fpix_blocks = unsigned((pl.npix + kFieldEwaldThreads - 1) / kFieldEwaldThreads);
+  const unsigned fpix_blocks = unsigned((pl.npix + 31) / 32);  // k_ewald_fields: 32 pixels per block
   const int W = int(pl.ny), H = int(pl.nx);  // the reference hands NPP width = Ny, height = Nx
   const unsigned rot_tiles = unsigned(((W + kRotTile - 1) / kRotTile) * ((H + kRotTile - 1) / kRotTile));
   const WarpCoef *dwarp = reinterpret_cast<const WarpCoef *>(dp + pl.off_warp);
@@ -1108,7 +1108,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
       rg.rows = pl.has_rows ? reinterpret_cast<const int2 *>(dp + pl.off_rows) + (size_t(k) * pl.ne + e0) * H : nullptr;
       const dim3 rgrid(rot_tiles, (nb + nep - 1) / nep);
       slot = ctx.prof.begin(kEwaldFields, st);
-      const unsigned fgrid = fpix_blocks * nb;
+      const unsigned fgrid = fpix_blocks * ((nb + kEwaldEnergies - 1) / kEwaldEnergies);
       if (pl.material_frame)
         k_ewald_fields<0><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
       else if (pl.nbasis == 2)

@@ -139,7 +139,8 @@ struct FieldEwaldParams {
   uint32_t nbatch;       // energies of this launch
 };
 
-constexpr int kFieldEwaldThreads = 128;
+constexpr int kEwaldEnergies = 4;  // energies (warps) per block
+constexpr int kFieldEwaldThreads = 32 * kEwaldEnergies;
 constexpr int kFieldGather = 4;  // packed volumes whose loads are issued together
 
 // NB = 2 or 3: LAB frame, Gram maps over the E basis (p(a) = sum_b E_b(a) Nt e_b),
@@ -149,13 +150,23 @@ constexpr int kFieldGather = 4;  // packed volumes whose loads are issued togeth
 // Ewald sphere) run together and share the gathered sectors in L2.
 template <int NB>
 __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldParams p) {
-  extern __shared__ float4 fcoef[];  // [6][npk]
-  const uint32_t eb = blockIdx.x % p.nbatch, e = p.e0 + eb;
+  // a block: 32 pixels x kEwaldEnergies neighbouring energies, one warp per
+  // energy, so the warps of an SM gather nearly the same sectors (their Ewald
+  // spheres almost coincide) and share them in L1
+  extern __shared__ float4 fcoef_all[];  // [kEwaldEnergies][6][npk]
+  const uint32_t ngrp = (p.nbatch + kEwaldEnergies - 1) / kEwaldEnergies;
+  const uint32_t warp = threadIdx.x >> 5;
+  const uint32_t eb = (blockIdx.x % ngrp) * kEwaldEnergies + warp, e = p.e0 + eb;
   const uint32_t nx = p.g.nx, ny = p.g.ny, nz = p.g.nz;
-  for (uint32_t t = threadIdx.x; t < 6 * p.npk; t += blockDim.x) fcoef[t] = p.coef[size_t(e) * 6 * p.npk + t];
+  for (uint32_t i = threadIdx.x; i < kEwaldEnergies * 6 * p.npk; i += blockDim.x) {
+    const uint32_t w = i / (6 * p.npk), eg = (blockIdx.x % ngrp) * kEwaldEnergies + w;
+    if (eg < p.nbatch) fcoef_all[i] = p.coef[size_t(p.e0 + eg) * 6 * p.npk + i % (6 * p.npk)];
+  }
   __syncthreads();
+  if (eb >= p.nbatch) return;
+  const float4 *fcoef = fcoef_all + warp * 6 * p.npk;
   const size_t npix = size_t(nx) * ny;
-  const size_t t = size_t(blockIdx.x / p.nbatch) * blockDim.x + threadIdx.x;
+  const size_t t = size_t(blockIdx.x / ngrp) * 32 + (threadIdx.x & 31);
   if (t >= npix) return;
   const uint32_t Y = uint32_t(t / nx), X = uint32_t(t % nx);
   EwaldGeom g = p.g;
