@@ -1196,7 +1196,9 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
     upload.host = mode.host_vox;
     upload.dev = const_cast<float4 *>(d_vox);
     upload.nmat = pl.nmat, upload.nz = pl.nz, upload.nvox = pl.nvox, upload.npix = pl.npix;
-    upload.count = pl.fields && pl.nz >= 8 ? 8u : 1u;
+    // slabs: after the last one lands, its fields and x/y passes are still ahead
+    // of the z pass, so thinner slabs shorten that tail
+    upload.count = !pl.fields ? 1u : pl.nz >= 64 ? 16u : pl.nz >= 8 ? 8u : 1u;
     upload.planes = (pl.nz + upload.count - 1) / upload.count;
     upload.count = (pl.nz + upload.planes - 1) / upload.planes;
     if (pl.fields) {
