@@ -227,6 +227,10 @@ struct DeviceContext {
   std::map<uint32_t, float2 *> twiddles;
   Scratch main;
   DeviceBuffer vox_in, out_in;  // host-buffer entry points: morphology and projections
+  // TMA column passes: the driver's tensor-map encoder, and a word set when a
+  // tile copy did not complete within the kernel's wait limit
+  void *encode_tiled = nullptr;
+  unsigned *tma_error = nullptr;
 };
 
 std::mutex g_ctx_mu;
@@ -282,6 +286,18 @@ int setup_attrs(DeviceContext &ctx) {
   CYR_WARP_Z_ATTR_V(16)
 #undef CYR_WARP_Z_ATTR_V
 #undef CYR_WARP_Z_ATTR
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cols_tma_smem(256))));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cols_tma_smem(512))));
+  {
+    cudaDriverEntryPointQueryResult q{};
+    void *fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      ctx.encode_tiled = fn;
+    cudaGetLastError();
+    CYR_CUDA(cudaMalloc(&ctx.tma_error, sizeof(unsigned)));
+    CYR_CUDA(cudaMemset(ctx.tma_error, 0, sizeof(unsigned)));
+  }
   ctx.attrs_done = true;
   return CYR_OK;
 }
@@ -331,6 +347,34 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     RowPassParams rp{data, uint32_t(size_t(ny) * nz * count), tw, ny * nz, nvox};
     const size_t smem = (N + 8 * N) * sizeof(float2);
     k_fft_rows<V><<<(rp.rows + 7) / 8, 256, smem, st>>>(rp);
+  } else if ((V == 8 || V == 16) && nx % kTmaCols == 0 && ctx.encode_tiled && ctx.tma_error) {
+    // TMA tiles: the tensor is (x, y, z, volume), a box of 16 columns x 256 lines
+    constexpr uint32_t BOX = N < 256 ? N : 256;
+    CUtensorMap map;
+    const cuuint64_t dims[4] = {nx, ny, nz, count};
+    const cuuint64_t strides[3] = {cuuint64_t(nx) * 8, cuuint64_t(nx) * ny * 8, cuuint64_t(nvox) * 8};
+    const cuuint32_t box[4] = {uint32_t(kTmaCols), axis == 1 ? BOX : 1u, axis == 2 ? BOX : 1u, 1u};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    const CUresult r = reinterpret_cast<Encode>(ctx.encode_tiled)(
+        &map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, data, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CYR_ERR_CUDA, "tensor map encoding failed (%d)", int(r));
+    ColTmaParams tp{};
+    tp.nxt = nx / kTmaCols;
+    tp.others = axis == 1 ? nz : ny;
+    tp.ntiles = tp.nxt * tp.others * count;
+    tp.axis = uint32_t(axis);
+    tp.tw = tw;
+    tp.error = ctx.tma_error;
+    int sms = 0, per_sm = 0;
+    CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+    CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma<V == 8 ? 8 : 16>, kTmaWarps * 32,
+                                                           cols_tma_smem(N)));
+    const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
+    k_fft_cols_tma<V == 8 ? 8 : 16><<<grid, kTmaWarps * 32, cols_tma_smem(N), st>>>(map, tp);
   } else {
     ColPassParams cp{};
     cp.data = data;
@@ -1955,6 +1999,9 @@ static int cuda_main_impl(const cyr_options *opt, const float *optical, const fl
     unsigned errs = 0;
     if (cudaMemcpy(&errs, ctx->main.errors.ptr, sizeof errs, cudaMemcpyDeviceToHost) == cudaSuccess && errs != 0)
       rc = fail(CYR_ERR_CUDA, "%u detector pixels needed z planes outside the kept range", errs);
+    if (ctx->tma_error && cudaMemcpy(&errs, ctx->tma_error, sizeof errs, cudaMemcpyDeviceToHost) == cudaSuccess &&
+        errs != 0)
+      rc = fail(CYR_ERR_CUDA, "an FFT tile copy did not complete within its wait limit");
   } while (false);
   cudaStreamSynchronize(cs);
   cudaStreamDestroy(cs);

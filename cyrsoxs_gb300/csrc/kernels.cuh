@@ -11,6 +11,7 @@
 // waits on another block.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (the type only; encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -775,6 +776,171 @@ __global__ void __launch_bounds__(TX * 32, cols_min_blocks(V, TX)) k_fft_cols(Co
       for (uint32_t i = i0; i < N; i += ISTEP) g[l + i * p.estride] = tile[l * L + swz(i)];
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Column pass over TMA tiles (y or z axis, lines of 256 or 512 points, nx a
+// multiple of 16).  Persistent blocks of 8 warps walk tiles of 16 adjacent
+// columns x N lines of one (plane or row, volume), double-buffered: the
+// tensor-memory accelerator loads tile k+1 (cp.async.bulk.tensor, completion
+// on an mbarrier) while tile k is transformed, and stores each finished tile
+// back with a bulk tensor store.  The tile lands with the 128-byte swizzle
+// (16-byte chunk c of line r at chunk c ^ (r & 7)), so warp w reads its two
+// columns 2w, 2w+1 as one 16-byte chunk per line, eight lines per
+// quarter-warp on eight distinct chunks: no bank conflicts, and no load/store
+// unit work for the tile copies at all.  Each warp transforms its two columns
+// with the warp FFT through its own exchange line.
+// ---------------------------------------------------------------------------
+constexpr int kTmaCols = 16;       // columns per tile (128 bytes per line)
+constexpr int kTmaWarps = kTmaCols / 2;
+
+struct ColTmaParams {
+  uint32_t ntiles;   // tiles in all volumes
+  uint32_t nxt;      // tiles across x (nx / 16)
+  uint32_t others;   // y pass: planes per volume; z pass: rows (ny)
+  uint32_t axis;     // 1: lines along y (tensor dim 1), 2: along z (dim 2)
+  const float2 *tw;  // twiddles of length N
+  unsigned *error;   // set to 1 when a tile copy did not complete within the wait limit
+};
+
+// Dynamic shared memory of k_fft_cols_tma: two tiles, the warps' exchange lines,
+// twiddles, two mbarriers, and slack to align the tiles to 1024 bytes.
+__host__ __device__ constexpr size_t cols_tma_smem(uint32_t n) {
+  return 2 * size_t(n) * kTmaCols * 8 + size_t(kTmaWarps) * n * 8 + size_t(n) * 8 + 16 + 1024;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// Waits for the phase with the given parity; false if it did not complete within `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];\n" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, int c0, int c1, int c2, int c3, const void *src) {
+  asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];\n" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+constexpr uint32_t kTmaWaitPolls = 1u << 22;  // each poll suspends up to a hardware time limit
+
+template <int V>
+__global__ void __launch_bounds__(kTmaWarps * 32, 1) k_fft_cols_tma(const __grid_constant__ CUtensorMap tmap,
+                                                                      ColTmaParams p) {
+  constexpr uint32_t N = 32 * V, TILE = N * kTmaCols;  // float2 per tile
+  constexpr uint32_t BOX = N < 256 ? N : 256, NBOX = N / BOX;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  float2 *tiles = reinterpret_cast<float2 *>(base);  // [2][N][16], swizzled
+  float2 *lines = tiles + 2 * TILE;                  // [warps][N]
+  float2 *tws = lines + kTmaWarps * N;               // [N]
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(tws + N);
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  warp_twiddles<V>(tws, p.tw);
+  __syncthreads();
+  auto coords = [&](uint32_t t, uint32_t b, int (&c)[4]) {
+    const uint32_t rest = t / p.nxt;
+    c[0] = int((t % p.nxt) * kTmaCols);
+    c[3] = int(rest / p.others);
+    if (p.axis == 1) {
+      c[1] = int(b * BOX), c[2] = int(rest % p.others);
+    } else {
+      c[1] = int(rest % p.others), c[2] = int(b * BOX);
+    }
+  };
+  auto issue_load = [&](uint32_t t, int s) {
+    mbar_expect_tx(&mbar[s], TILE * 8);
+#pragma unroll
+    for (uint32_t b = 0; b < NBOX; ++b) {
+      int c[4];
+      coords(t, b, c);
+      tma_load_4d(tiles + s * TILE + b * BOX * kTmaCols, &tmap, c[0], c[1], c[2], c[3], &mbar[s]);
+    }
+  };
+  uint32_t t = blockIdx.x, k = 0;
+  if (threadIdx.x == 0 && t < p.ntiles) issue_load(t, 0);
+  float2 *line = lines + warp * N;
+  for (; t < p.ntiles; t += gridDim.x, ++k) {
+    const int s = int(k & 1u);
+    if (threadIdx.x == 0 && t + gridDim.x < p.ntiles) {
+      bulk_wait_read_all();  // the store from the other stage has read its tile
+      issue_load(t + gridDim.x, s ^ 1);
+    }
+    const bool ok = mbar_wait(&mbar[s], (k >> 1) & 1u, kTmaWaitPolls);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(p.error, 1u);
+        // let the copies in flight land (bounded) before the block releases its shared memory
+        mbar_wait(&mbar[s], (k >> 1) & 1u, kTmaWaitPolls);
+        if (t + gridDim.x < p.ntiles) mbar_wait(&mbar[s ^ 1], ((k + 1) >> 1) & 1u, kTmaWaitPolls);
+      }
+      break;
+    }
+    unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE);
+    float2 a[V], c2[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const uint32_t r = lane + 32 * i;
+      const float4 q = *reinterpret_cast<const float4 *>(tb + r * 128 + ((warp ^ (r & 7u)) << 4));
+      a[i] = make_float2(q.x, q.y);
+      c2[i] = make_float2(q.z, q.w);
+    }
+    warp_fft<V>(a, line, tws, lane);
+    warp_fft<V>(c2, line, tws, lane);
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const uint32_t r = lane + 32 * i;
+      *reinterpret_cast<float4 *>(tb + r * 128 + ((warp ^ (r & 7u)) << 4)) =
+          make_float4(a[i].x, a[i].y, c2[i].x, c2[i].y);
+    }
+    fence_proxy_async();  // the generic-proxy writes become visible to the bulk store
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (uint32_t b = 0; b < NBOX; ++b) {
+        int c[4];
+        coords(t, b, c);
+        tma_store_4d(&tmap, c[0], c[1], c[2], c[3], tiles + s * TILE + b * BOX * kTmaCols);
+      }
+      bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 // Per-thread register FFT for short strided lines (N = 8..64, powers of two):
