@@ -287,7 +287,8 @@ int setup_attrs(DeviceContext &ctx) {
 #undef CYR_WARP_Z_ATTR_V
 #undef CYR_WARP_Z_ATTR
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cols_tma_smem(256))));
-  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cols_tma_smem(512))));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(cols_tma_smem(512))));
   {
     cudaDriverEntryPointQueryResult q{};
     void *fn = nullptr;
@@ -371,10 +372,17 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     tp.error = ctx.tma_error;
     int sms = 0, per_sm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
-    CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma<V == 8 ? 8 : 16>, kTmaWarps * 32,
-                                                           cols_tma_smem(N)));
-    const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
-    k_fft_cols_tma<V == 8 ? 8 : 16><<<grid, kTmaWarps * 32, cols_tma_smem(N), st>>>(map, tp);
+    // 256-point lines: block-synchronous form; 512: with a producer warp (the faster of each)
+    if constexpr (V == 8) {
+      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma<8>, kTmaWarps * 32, cols_tma_smem(N)));
+      const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
+      k_fft_cols_tma<8><<<grid, kTmaWarps * 32, cols_tma_smem(N), st>>>(map, tp);
+    } else {
+      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<16>, (kTmaWarps + 1) * 32,
+                                                             cols_tma_smem(N)));
+      const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
+      k_fft_cols_tma_ws<16><<<grid, (kTmaWarps + 1) * 32, cols_tma_smem(N), st>>>(map, tp);
+    }
   } else {
     ColPassParams cp{};
     cp.data = data;

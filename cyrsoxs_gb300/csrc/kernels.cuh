@@ -789,7 +789,8 @@ __global__ void __launch_bounds__(TX * 32, cols_min_blocks(V, TX)) k_fft_cols(Co
 // columns 2w, 2w+1 as one 16-byte chunk per line, eight lines per
 // quarter-warp on eight distinct chunks: no bank conflicts, and no load/store
 // unit work for the tile copies at all.  Each warp transforms its two columns
-// with the warp FFT through its own exchange line.
+// with the warp FFT through its own exchange line.  (One column per warp, 16
+// warps, measured slower: its 8-byte reads put two lanes on each bank pair.)
 // ---------------------------------------------------------------------------
 constexpr int kTmaCols = 16;       // columns per tile (128 bytes per line)
 constexpr int kTmaWarps = kTmaCols / 2;
@@ -806,7 +807,7 @@ struct ColTmaParams {
 // Dynamic shared memory of k_fft_cols_tma: two tiles, the warps' exchange lines,
 // twiddles, two mbarriers, and slack to align the tiles to 1024 bytes.
 __host__ __device__ constexpr size_t cols_tma_smem(uint32_t n) {
-  return 2 * size_t(n) * kTmaCols * 8 + size_t(kTmaWarps) * n * 8 + size_t(n) * 8 + 16 + 1024;
+  return 2 * size_t(n) * kTmaCols * 8 + size_t(kTmaWarps) * n * 8 + size_t(n) * 8 + 32 + 1024;
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -854,6 +855,7 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 
 constexpr uint32_t kTmaWaitPolls = 1u << 22;  // each poll suspends up to a hardware time limit
 
+// Block-synchronous form: thread 0 issues the copies between the tiles' compute phases.
 template <int V>
 __global__ void __launch_bounds__(kTmaWarps * 32, 1) k_fft_cols_tma(const __grid_constant__ CUtensorMap tmap,
                                                                       ColTmaParams p) {
@@ -941,6 +943,120 @@ __global__ void __launch_bounds__(kTmaWarps * 32, 1) k_fft_cols_tma(const __grid
     }
   }
   if (threadIdx.x == 0) bulk_wait_all();
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Warp-specialised form (512-point lines; for 256 points the block-synchronous
+// k_fft_cols_tma measured faster): warps 0..7 transform (two columns each),
+// warp 8 is the producer.  Per stage s: full[s] completes when a tile's copy has landed
+// (transaction count), empty[s] when the 8 compute warps are done with it.
+// The producer stores a finished tile as soon as empty[s] completes, and
+// reloads the stage once that store has read it; the compute warps never wait
+// on the copies' shared-memory reads and never meet at a block barrier.
+template <int V>
+__global__ void __launch_bounds__((kTmaWarps + 1) * 32, 1) k_fft_cols_tma_ws(const __grid_constant__ CUtensorMap tmap,
+                                                                               ColTmaParams p) {
+  constexpr uint32_t N = 32 * V, TILE = N * kTmaCols;  // float2 per tile
+  constexpr uint32_t BOX = N < 256 ? N : 256, NBOX = N / BOX;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  float2 *tiles = reinterpret_cast<float2 *>(base);  // [2][N][16], swizzled
+  float2 *lines = tiles + 2 * TILE;                  // [compute warps][N]
+  float2 *tws = lines + kTmaWarps * N;               // [N]
+  uint64_t *full = reinterpret_cast<uint64_t *>(tws + N), *empty = full + 2;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(&empty[0], kTmaWarps);
+    mbar_init(&empty[1], kTmaWarps);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  warp_twiddles<V>(tws, p.tw);
+  __syncthreads();
+  auto coords = [&](uint32_t t, uint32_t b, int (&c)[4]) {
+    const uint32_t rest = t / p.nxt;
+    c[0] = int((t % p.nxt) * kTmaCols);
+    c[3] = int(rest / p.others);
+    if (p.axis == 1) {
+      c[1] = int(b * BOX), c[2] = int(rest % p.others);
+    } else {
+      c[1] = int(rest % p.others), c[2] = int(b * BOX);
+    }
+  };
+  if (warp == kTmaWarps) {  // producer
+    if (lane != 0) return;
+    auto store = [&](uint32_t t, int s) {
+#pragma unroll
+      for (uint32_t b = 0; b < NBOX; ++b) {
+        int c[4];
+        coords(t, b, c);
+        tma_store_4d(&tmap, c[0], c[1], c[2], c[3], tiles + s * TILE + b * BOX * kTmaCols);
+      }
+      bulk_commit();
+    };
+    bool ok = true;
+    uint32_t k = 0;
+    for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x, ++k) {
+      const int s = int(k & 1u);
+      if (k >= 2) {  // tile k-2 occupies stage s: store it, let the store read it, then reload
+        ok = mbar_wait(&empty[s], ((k >> 1) - 1) & 1u, kTmaWaitPolls);
+        if (!ok) break;
+        store(t - 2 * gridDim.x, s);
+        bulk_wait_read_all();
+      }
+      mbar_expect_tx(&full[s], TILE * 8);
+#pragma unroll
+      for (uint32_t b = 0; b < NBOX; ++b) {
+        int c[4];
+        coords(t, b, c);
+        tma_load_4d(tiles + s * TILE + b * BOX * kTmaCols, &tmap, c[0], c[1], c[2], c[3], &full[s]);
+      }
+    }
+    // the last (up to) two tiles
+    const uint32_t ntile = p.ntiles > blockIdx.x ? (p.ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
+    for (uint32_t kk = ntile >= 2 ? ntile - 2 : 0u; ok && kk < ntile; ++kk) {
+      const int s = int(kk & 1u);
+      ok = mbar_wait(&empty[s], (kk >> 1) & 1u, kTmaWaitPolls);
+      if (ok) store(blockIdx.x + kk * gridDim.x, s);
+    }
+    if (!ok) atomicExch(p.error, 1u);
+    bulk_wait_all();
+    return;
+  }
+  // compute warps
+  float2 *line = lines + warp * N;
+  uint32_t k = 0;
+  for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++k) {
+    const int s = int(k & 1u);
+    if (!mbar_wait(&full[s], (k >> 1) & 1u, kTmaWaitPolls)) {
+      if (lane == 0) atomicExch(p.error, 1u);
+      return;
+    }
+    unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE);
+    float2 a[V], c2[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const uint32_t r = lane + 32 * i;
+      const float4 q = *reinterpret_cast<const float4 *>(tb + r * 128 + ((warp ^ (r & 7u)) << 4));
+      a[i] = make_float2(q.x, q.y);
+      c2[i] = make_float2(q.z, q.w);
+    }
+    warp_fft<V>(a, line, tws, lane);
+    warp_fft<V>(c2, line, tws, lane);
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const uint32_t r = lane + 32 * i;
+      *reinterpret_cast<float4 *>(tb + r * 128 + ((warp ^ (r & 7u)) << 4)) =
+          make_float4(a[i].x, a[i].y, c2[i].x, c2[i].y);
+    }
+    fence_proxy_async();  // the generic-proxy writes become visible to the bulk store
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
 }
 
 // Per-thread register FFT for short strided lines (N = 8..64, powers of two):
