@@ -287,8 +287,10 @@ int setup_attrs(DeviceContext &ctx) {
 #undef CYR_WARP_Z_ATTR_V
 #undef CYR_WARP_Z_ATTR
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cols_tma_smem(256))));
-  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(cols_tma_smem(512))));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(cols_tma_ws_smem<1>(512))));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(cols_tma_ws_smem<2>(256))));
   {
     cudaDriverEntryPointQueryResult q{};
     void *fn = nullptr;
@@ -372,16 +374,27 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     tp.error = ctx.tma_error;
     int sms = 0, per_sm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
-    // 256-point lines: block-synchronous form; 512: with a producer warp (the faster of each)
+    // 256-point lines: tiles of 32 columns with a producer warp (nx a multiple of
+    // 32; 256-byte runs per line), else the block-synchronous 16-column form;
+    // 512-point lines: 16 columns with a producer warp
     if constexpr (V == 8) {
-      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma<8>, kTmaWarps * 32, cols_tma_smem(N)));
-      const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
-      k_fft_cols_tma<8><<<grid, kTmaWarps * 32, cols_tma_smem(N), st>>>(map, tp);
+      if (nx % (2 * kTmaCols) == 0) {
+        tp.nxt = nx / (2 * kTmaCols);
+        tp.ntiles = tp.nxt * tp.others * count;
+        CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<8, 2>, 17 * 32,
+                                                               cols_tma_ws_smem<2>(N)));
+        const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
+        k_fft_cols_tma_ws<8, 2><<<grid, 17 * 32, cols_tma_ws_smem<2>(N), st>>>(map, tp);
+      } else {
+        CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma<8>, kTmaWarps * 32, cols_tma_smem(N)));
+        const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
+        k_fft_cols_tma<8><<<grid, kTmaWarps * 32, cols_tma_smem(N), st>>>(map, tp);
+      }
     } else {
-      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<16>, (kTmaWarps + 1) * 32,
-                                                             cols_tma_smem(N)));
+      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<16, 1>, 9 * 32,
+                                                             cols_tma_ws_smem<1>(N)));
       const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
-      k_fft_cols_tma_ws<16><<<grid, (kTmaWarps + 1) * 32, cols_tma_smem(N), st>>>(map, tp);
+      k_fft_cols_tma_ws<16, 1><<<grid, 9 * 32, cols_tma_ws_smem<1>(N), st>>>(map, tp);
     }
   } else {
     ColPassParams cp{};

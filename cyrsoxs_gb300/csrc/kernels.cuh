@@ -949,37 +949,43 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Warp-specialised form (512-point lines; for 256 points the block-synchronous
-// k_fft_cols_tma measured faster): warps 0..7 transform (two columns each),
-// warp 8 is the producer.  Per stage s: full[s] completes when a tile's copy has landed
-// (transaction count), empty[s] when the 8 compute warps are done with it.
-// The producer stores a finished tile as soon as empty[s] completes, and
+// Warp-specialised form: H halves of 16 columns per tile (each its own
+// swizzled N x 128-byte region), 8 H compute warps (two columns each) and a
+// producer warp.  Per stage s: full[s] completes when a tile's copies have
+// landed (transaction count), empty[s] when the compute warps are done with
+// it.  The producer stores a finished tile as soon as empty[s] completes and
 // reloads the stage once that store has read it; the compute warps never wait
 // on the copies' shared-memory reads and never meet at a block barrier.
-template <int V>
-__global__ void __launch_bounds__((kTmaWarps + 1) * 32, 1) k_fft_cols_tma_ws(const __grid_constant__ CUtensorMap tmap,
-                                                                               ColTmaParams p) {
-  constexpr uint32_t N = 32 * V, TILE = N * kTmaCols;  // float2 per tile
-  constexpr uint32_t BOX = N < 256 ? N : 256, NBOX = N / BOX;
+template <int H>
+__host__ __device__ constexpr size_t cols_tma_ws_smem(uint32_t n) {
+  return 2 * size_t(H) * n * kTmaCols * 8 + size_t(8 * H) * n * 8 + size_t(n) * 8 + 32 + 1024;
+}
+
+template <int V, int H>
+__global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const __grid_constant__ CUtensorMap tmap,
+                                                                          ColTmaParams p) {
+  constexpr uint32_t N = 32 * V, HALF = N * kTmaCols, TILE = H * HALF;  // float2 per half / tile
+  constexpr uint32_t BOX = N < 256 ? N : 256, NBOX = N / BOX, NW = 8 * H;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  float2 *tiles = reinterpret_cast<float2 *>(base);  // [2][N][16], swizzled
+  float2 *tiles = reinterpret_cast<float2 *>(base);  // [2][H][N][16], each half swizzled
   float2 *lines = tiles + 2 * TILE;                  // [compute warps][N]
-  float2 *tws = lines + kTmaWarps * N;               // [N]
+  float2 *tws = lines + NW * N;                      // [N]
   uint64_t *full = reinterpret_cast<uint64_t *>(tws + N), *empty = full + 2;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     mbar_init(&full[0], 1);
     mbar_init(&full[1], 1);
-    mbar_init(&empty[0], kTmaWarps);
-    mbar_init(&empty[1], kTmaWarps);
+    mbar_init(&empty[0], NW);
+    mbar_init(&empty[1], NW);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   warp_twiddles<V>(tws, p.tw);
   __syncthreads();
-  auto coords = [&](uint32_t t, uint32_t b, int (&c)[4]) {
+  // p.nxt counts tiles of H * 16 columns
+  auto coords = [&](uint32_t t, uint32_t h, uint32_t b, int (&c)[4]) {
     const uint32_t rest = t / p.nxt;
-    c[0] = int((t % p.nxt) * kTmaCols);
+    c[0] = int(((t % p.nxt) * H + h) * kTmaCols);
     c[3] = int(rest / p.others);
     if (p.axis == 1) {
       c[1] = int(b * BOX), c[2] = int(rest % p.others);
@@ -987,15 +993,18 @@ __global__ void __launch_bounds__((kTmaWarps + 1) * 32, 1) k_fft_cols_tma_ws(con
       c[1] = int(rest % p.others), c[2] = int(b * BOX);
     }
   };
-  if (warp == kTmaWarps) {  // producer
+  auto region = [&](int s, uint32_t h, uint32_t b) { return tiles + s * TILE + h * HALF + b * BOX * kTmaCols; };
+  if (warp == NW) {  // producer
     if (lane != 0) return;
     auto store = [&](uint32_t t, int s) {
 #pragma unroll
-      for (uint32_t b = 0; b < NBOX; ++b) {
-        int c[4];
-        coords(t, b, c);
-        tma_store_4d(&tmap, c[0], c[1], c[2], c[3], tiles + s * TILE + b * BOX * kTmaCols);
-      }
+      for (uint32_t h = 0; h < H; ++h)
+#pragma unroll
+        for (uint32_t b = 0; b < NBOX; ++b) {
+          int c[4];
+          coords(t, h, b, c);
+          tma_store_4d(&tmap, c[0], c[1], c[2], c[3], region(s, h, b));
+        }
       bulk_commit();
     };
     bool ok = true;
@@ -1010,11 +1019,13 @@ __global__ void __launch_bounds__((kTmaWarps + 1) * 32, 1) k_fft_cols_tma_ws(con
       }
       mbar_expect_tx(&full[s], TILE * 8);
 #pragma unroll
-      for (uint32_t b = 0; b < NBOX; ++b) {
-        int c[4];
-        coords(t, b, c);
-        tma_load_4d(tiles + s * TILE + b * BOX * kTmaCols, &tmap, c[0], c[1], c[2], c[3], &full[s]);
-      }
+      for (uint32_t h = 0; h < H; ++h)
+#pragma unroll
+        for (uint32_t b = 0; b < NBOX; ++b) {
+          int c[4];
+          coords(t, h, b, c);
+          tma_load_4d(region(s, h, b), &tmap, c[0], c[1], c[2], c[3], &full[s]);
+        }
     }
     // the last (up to) two tiles
     const uint32_t ntile = p.ntiles > blockIdx.x ? (p.ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
@@ -1027,8 +1038,9 @@ __global__ void __launch_bounds__((kTmaWarps + 1) * 32, 1) k_fft_cols_tma_ws(con
     bulk_wait_all();
     return;
   }
-  // compute warps
+  // compute warps: warp w owns columns 2 (w % 8), 2 (w % 8) + 1 of half w / 8
   float2 *line = lines + warp * N;
+  const uint32_t cw = warp & 7u, hw = warp >> 3;
   uint32_t k = 0;
   for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++k) {
     const int s = int(k & 1u);
@@ -1036,12 +1048,12 @@ __global__ void __launch_bounds__((kTmaWarps + 1) * 32, 1) k_fft_cols_tma_ws(con
       if (lane == 0) atomicExch(p.error, 1u);
       return;
     }
-    unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE);
+    unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE + hw * HALF);
     float2 a[V], c2[V];
 #pragma unroll
     for (int i = 0; i < V; ++i) {
       const uint32_t r = lane + 32 * i;
-      const float4 q = *reinterpret_cast<const float4 *>(tb + r * 128 + ((warp ^ (r & 7u)) << 4));
+      const float4 q = *reinterpret_cast<const float4 *>(tb + r * 128 + ((cw ^ (r & 7u)) << 4));
       a[i] = make_float2(q.x, q.y);
       c2[i] = make_float2(q.z, q.w);
     }
@@ -1050,7 +1062,7 @@ __global__ void __launch_bounds__((kTmaWarps + 1) * 32, 1) k_fft_cols_tma_ws(con
 #pragma unroll
     for (int i = 0; i < V; ++i) {
       const uint32_t r = lane + 32 * i;
-      *reinterpret_cast<float4 *>(tb + r * 128 + ((warp ^ (r & 7u)) << 4)) =
+      *reinterpret_cast<float4 *>(tb + r * 128 + ((cw ^ (r & 7u)) << 4)) =
           make_float4(a[i].x, a[i].y, c2[i].x, c2[i].y);
     }
     fence_proxy_async();  // the generic-proxy writes become visible to the bulk store
