@@ -78,6 +78,7 @@ def lib():
     L.cyr_required_device_bytes.argtypes = [opt_p, ctypes.POINTER(ctypes.c_size_t)]
     L.cyr_fft3d_device.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.c_void_p]
+    L.cyr_selftest_wait_limit.argtypes = [ctypes.POINTER(ctypes.c_int)]
     L.cyr_fft3d_device_static.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                           ctypes.c_uint32, ctypes.c_void_p]
     L.cyr_warp_affine_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
@@ -180,6 +181,13 @@ def required_device_bytes(opts: Options) -> int:
 def simulate_device(opts: Options, optical: np.ndarray, d_voxels: int, d_out: int, stream: int = 0) -> None:
     check(lib().cyr_simulate_device(opts.ref, fptr(np.ascontiguousarray(optical, np.float32)), ctypes.c_void_p(d_voxels),
                                     ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
+
+
+def selftest_wait_limit() -> bool:
+    """Runs the TMA column pass with a barrier that can never complete; True if its bounded waits reported it."""
+    flag = ctypes.c_int(0)
+    check(lib().cyr_selftest_wait_limit(ctypes.byref(flag)))
+    return bool(flag.value)
 
 
 def fft3d_device(d_data: int, nx: int, ny: int, nz: int, count: int = 1, stream: int = 0) -> None:

@@ -338,6 +338,25 @@ int make_axis(DeviceContext &ctx, uint32_t n, FftAxis &ax) {
   return get_twiddles(ctx, n, &ax.tw);
 }
 
+// Tensor map of `count` float2 volumes seen as (x, y, z, volume), volumes nvox
+// elements apart, for TMA tiles of 16 columns x `box` lines along `axis`
+// (1: y, 2: z), 128-byte swizzle.
+int encode_cols_map(DeviceContext &ctx, CUtensorMap *map, void *data, uint32_t nx, uint32_t ny, uint32_t nz,
+                    uint32_t count, size_t nvox, int axis, uint32_t box) {
+  const cuuint64_t dims[4] = {nx, ny, nz, count};
+  const cuuint64_t strides[3] = {cuuint64_t(nx) * 8, cuuint64_t(nx) * ny * 8, cuuint64_t(nvox) * 8};
+  const cuuint32_t boxd[4] = {uint32_t(kTmaCols), axis == 1 ? box : 1u, axis == 2 ? box : 1u, 1u};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  const CUresult r = reinterpret_cast<Encode>(ctx.encode_tiled)(
+      map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, data, dims, strides, boxd, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(CYR_ERR_CUDA, "tensor map encoding failed (%d)", int(r));
+  return CYR_OK;
+}
+
 // One axis of the 3D FFT with the warp-level kernels (n = 128, 256, 512).
 template <int V>
 int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
@@ -351,20 +370,8 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     const size_t smem = (N + 8 * N) * sizeof(float2);
     k_fft_rows<V><<<(rp.rows + 7) / 8, 256, smem, st>>>(rp);
   } else if ((V == 8 || V == 16) && nx % kTmaCols == 0 && ctx.encode_tiled && ctx.tma_error) {
-    // TMA tiles: the tensor is (x, y, z, volume), a box of 16 columns x 256 lines
-    constexpr uint32_t BOX = N < 256 ? N : 256;
     CUtensorMap map;
-    const cuuint64_t dims[4] = {nx, ny, nz, count};
-    const cuuint64_t strides[3] = {cuuint64_t(nx) * 8, cuuint64_t(nx) * ny * 8, cuuint64_t(nvox) * 8};
-    const cuuint32_t box[4] = {uint32_t(kTmaCols), axis == 1 ? BOX : 1u, axis == 2 ? BOX : 1u, 1u};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-    const CUresult r = reinterpret_cast<Encode>(ctx.encode_tiled)(
-        &map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, data, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(CYR_ERR_CUDA, "tensor map encoding failed (%d)", int(r));
+    CYR_TRY(encode_cols_map(ctx, &map, data, nx, ny, nz, count, nvox, axis, N < 256 ? N : 256));
     ColTmaParams tp{};
     tp.nxt = nx / kTmaCols;
     tp.others = axis == 1 ? nz : ny;
@@ -2162,6 +2169,49 @@ int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32
   std::lock_guard<std::mutex> lk(ctx->mu);
   CYR_TRY(setup_attrs(*ctx));
   return fft3d(*ctx, static_cast<float2 *>(d_data), nx, ny, nz, count, static_cast<cudaStream_t>(stream));
+}
+
+int cyr_selftest_wait_limit(int *timed_out) {
+  if (!timed_out) return fail(CYR_ERR_ARGUMENT, "timed_out pointer is null");
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CYR_TRY(setup_attrs(*ctx));
+  if (!ctx->encode_tiled) return fail(CYR_ERR_UNSUPPORTED, "no tensor-map encoder in this driver");
+  // one 32-column x 256-line tile; its copies deliver 16 bytes fewer than the
+  // barrier expects, so the phase never completes and every wait runs out
+  constexpr uint32_t nx = 32, ny = 256;
+  const float2 *tw = nullptr;
+  CYR_TRY(get_twiddles(*ctx, ny, &tw));
+  float2 *d = nullptr;
+  CYR_CUDA(cudaMalloc(&d, size_t(nx) * ny * sizeof(float2)));
+  int rc = CYR_OK;
+  do {
+    CUtensorMap map;
+    if ((rc = encode_cols_map(*ctx, &map, d, nx, ny, 1, 1, size_t(nx) * ny, 1, ny)) != CYR_OK) break;
+    ColTmaParams tp{};
+    tp.nxt = 1, tp.others = 1, tp.ntiles = 1, tp.axis = 1;
+    tp.tw = tw;
+    tp.error = ctx->tma_error;
+    tp.poll_limit = 1u << 16;  // far longer than the 64 KB copies take to land
+    tp.extra_tx = 16;
+    if (cudaMemset(d, 0, size_t(nx) * ny * sizeof(float2)) != cudaSuccess ||
+        cudaMemset(ctx->tma_error, 0, sizeof(unsigned)) != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "self-test setup failed");
+      break;
+    }
+    k_fft_cols_tma_ws<8, 2><<<1, 17 * 32, cols_tma_ws_smem<2>(ny)>>>(map, tp);
+    const cudaError_t e = cudaDeviceSynchronize();
+    unsigned flag = 0;
+    if (e != cudaSuccess || cudaMemcpy(&flag, ctx->tma_error, sizeof flag, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "self-test kernel failed: %s", cudaGetErrorString(e));
+      break;
+    }
+    *timed_out = flag != 0;
+    if (cudaMemset(ctx->tma_error, 0, sizeof(unsigned)) != cudaSuccess) rc = fail(CYR_ERR_CUDA, "flag reset failed");
+  } while (false);
+  cudaFree(d);
+  return rc;
 }
 
 int cyr_warp_affine_device(const float *d_src, float *d_dst, int width, int height, const double *coeffs,

@@ -802,6 +802,9 @@ struct ColTmaParams {
   uint32_t axis;     // 1: lines along y (tensor dim 1), 2: along z (dim 2)
   const float2 *tw;  // twiddles of length N
   unsigned *error;   // set to 1 when a tile copy did not complete within the wait limit
+  // self-test of the bounded waits (cyr_selftest_wait_limit); 0 in normal use:
+  uint32_t poll_limit;  // polls per wait (0: kTmaWaitPolls)
+  uint32_t extra_tx;    // bytes expected beyond the tile's, so its phase never completes
 };
 
 // Dynamic shared memory of k_fft_cols_tma: two tiles, the warps' exchange lines,
@@ -886,7 +889,7 @@ __global__ void __launch_bounds__(kTmaWarps * 32, 1) k_fft_cols_tma(const __grid
     }
   };
   auto issue_load = [&](uint32_t t, int s) {
-    mbar_expect_tx(&mbar[s], TILE * 8);
+    mbar_expect_tx(&mbar[s], TILE * 8 + p.extra_tx);
 #pragma unroll
     for (uint32_t b = 0; b < NBOX; ++b) {
       int c[4];
@@ -903,13 +906,14 @@ __global__ void __launch_bounds__(kTmaWarps * 32, 1) k_fft_cols_tma(const __grid
       bulk_wait_read_all();  // the store from the other stage has read its tile
       issue_load(t + gridDim.x, s ^ 1);
     }
-    const bool ok = mbar_wait(&mbar[s], (k >> 1) & 1u, kTmaWaitPolls);
+    const uint32_t limit = p.poll_limit ? p.poll_limit : kTmaWaitPolls;
+    const bool ok = mbar_wait(&mbar[s], (k >> 1) & 1u, limit);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
         atomicExch(p.error, 1u);
         // let the copies in flight land (bounded) before the block releases its shared memory
-        mbar_wait(&mbar[s], (k >> 1) & 1u, kTmaWaitPolls);
-        if (t + gridDim.x < p.ntiles) mbar_wait(&mbar[s ^ 1], ((k + 1) >> 1) & 1u, kTmaWaitPolls);
+        mbar_wait(&mbar[s], (k >> 1) & 1u, limit);
+        if (t + gridDim.x < p.ntiles) mbar_wait(&mbar[s ^ 1], ((k + 1) >> 1) & 1u, limit);
       }
       break;
     }
@@ -1009,15 +1013,18 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
     };
     bool ok = true;
     uint32_t k = 0;
+    const uint32_t limit = p.poll_limit ? p.poll_limit : kTmaWaitPolls;
+    int last[2] = {-1, -1};  // last tile index loaded into each stage
     for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x, ++k) {
       const int s = int(k & 1u);
       if (k >= 2) {  // tile k-2 occupies stage s: store it, let the store read it, then reload
-        ok = mbar_wait(&empty[s], ((k >> 1) - 1) & 1u, kTmaWaitPolls);
+        ok = mbar_wait(&empty[s], ((k >> 1) - 1) & 1u, limit);
         if (!ok) break;
         store(t - 2 * gridDim.x, s);
         bulk_wait_read_all();
       }
-      mbar_expect_tx(&full[s], TILE * 8);
+      mbar_expect_tx(&full[s], TILE * 8 + p.extra_tx);
+      last[s] = int(k);
 #pragma unroll
       for (uint32_t h = 0; h < H; ++h)
 #pragma unroll
@@ -1031,20 +1038,26 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
     const uint32_t ntile = p.ntiles > blockIdx.x ? (p.ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
     for (uint32_t kk = ntile >= 2 ? ntile - 2 : 0u; ok && kk < ntile; ++kk) {
       const int s = int(kk & 1u);
-      ok = mbar_wait(&empty[s], (kk >> 1) & 1u, kTmaWaitPolls);
+      ok = mbar_wait(&empty[s], (kk >> 1) & 1u, limit);
       if (ok) store(blockIdx.x + kk * gridDim.x, s);
     }
-    if (!ok) atomicExch(p.error, 1u);
+    if (!ok) {
+      atomicExch(p.error, 1u);
+      // the block must not release its shared memory under copies still landing
+      for (int st = 0; st < 2; ++st)
+        if (last[st] >= 0) mbar_wait(&full[st], (uint32_t(last[st]) >> 1) & 1u, limit);
+    }
     bulk_wait_all();
     return;
   }
   // compute warps: warp w owns columns 2 (w % 8), 2 (w % 8) + 1 of half w / 8
   float2 *line = lines + warp * N;
   const uint32_t cw = warp & 7u, hw = warp >> 3;
+  const uint32_t limit = p.poll_limit ? p.poll_limit : kTmaWaitPolls;
   uint32_t k = 0;
   for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++k) {
     const int s = int(k & 1u);
-    if (!mbar_wait(&full[s], (k >> 1) & 1u, kTmaWaitPolls)) {
+    if (!mbar_wait(&full[s], (k >> 1) & 1u, limit)) {
       if (lane == 0) atomicExch(p.error, 1u);
       return;
     }

@@ -175,6 +175,15 @@ CYR_API int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, uint
                                     void *stream);
 
 /*
+ * cyr_selftest_wait_limit: checks the bounded waits of the TMA column FFT pass.
+ * It runs that kernel once on a 32 x 256 tile whose copies deliver fewer bytes
+ * than the kernel's barrier expects, so every wait runs out; the kernel must
+ * report it (*timed_out = 1), wait for its copies, and leave the context
+ * usable.  Synchronises the device.  No counterpart in the reference.
+ */
+CYR_API int cyr_selftest_wait_limit(int *timed_out);
+
+/*
  * cyr_warp_affine_device: bilinear affine warp of a float [height][width]
  * image with the semantics of nppiWarpAffine_32f_C1R + NPPI_INTER_LINEAR
  * (src/cudaMain.cu:91-121, :858, :943).  coeffs is the 2x3 matrix mapping

@@ -57,7 +57,10 @@ def rel_err(a, ref, thr=1e-6):
                                          ((32, 256, 256), 1), ((9, 25, 49), 1), ((3, 128, 512), 2),
                                          ((128, 20, 24), 1), ((256, 6, 40), 1), ((512, 512, 8), 1),
                                          ((2, 512, 128), 3), ((2, 8, 1024), 2), ((4, 1024, 24), 1), ((1024, 4, 40), 1),
-                                         ((16, 64, 40), 2), ((32, 8, 16), 1)])
+                                         ((16, 64, 40), 2), ((32, 8, 16), 1),
+                                         # TMA column passes: 32-column tiles, 16-column tiles (nx not a
+                                         # multiple of 32), 512-point lines on several volumes
+                                         ((4, 256, 64), 2), ((256, 4, 48), 1), ((2, 256, 80), 2), ((2, 512, 16), 3)])
 def test_fft3d_matches_numpy(shape, count):
     torch = _torch()
     nat = native()
@@ -71,6 +74,17 @@ def test_fft3d_matches_numpy(shape, count):
     ref = np.fft.fftn(a.astype(np.complex128), axes=(1, 2, 3))
     err = np.abs(got - ref).max() / np.abs(ref).max()
     assert err < 2e-6, err
+
+
+def test_tma_wait_limit_reports_and_recovers():
+    """The TMA column pass bounds every barrier wait.  A tile whose copies
+    deliver fewer bytes than the barrier expects never completes: the kernel
+    must give up, report it, let its copies land, and leave the context usable
+    for the transforms that follow."""
+    _torch()
+    nat = native()
+    assert nat.selftest_wait_limit() is True
+    test_fft3d_matches_numpy((4, 256, 64), 2)
 
 
 def test_warp_is_bit_exact_with_npp_probes():
