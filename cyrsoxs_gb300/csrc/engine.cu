@@ -291,6 +291,8 @@ int setup_attrs(DeviceContext &ctx) {
                                 int(cols_tma_ws_smem<1>(512))));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(cols_tma_ws_smem<2>(256))));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma64<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(cols_tma64_smem(1024))));
   {
     cudaDriverEntryPointQueryResult q{};
     void *fn = nullptr;
@@ -342,17 +344,18 @@ int make_axis(DeviceContext &ctx, uint32_t n, FftAxis &ax) {
 // elements apart, for TMA tiles of 16 columns x `box` lines along `axis`
 // (1: y, 2: z), 128-byte swizzle.
 int encode_cols_map(DeviceContext &ctx, CUtensorMap *map, void *data, uint32_t nx, uint32_t ny, uint32_t nz,
-                    uint32_t count, size_t nvox, int axis, uint32_t box) {
+                    uint32_t count, size_t nvox, int axis, uint32_t box, uint32_t cols = kTmaCols) {
   const cuuint64_t dims[4] = {nx, ny, nz, count};
   const cuuint64_t strides[3] = {cuuint64_t(nx) * 8, cuuint64_t(nx) * ny * 8, cuuint64_t(nvox) * 8};
-  const cuuint32_t boxd[4] = {uint32_t(kTmaCols), axis == 1 ? box : 1u, axis == 2 ? box : 1u, 1u};
+  const cuuint32_t boxd[4] = {cols, axis == 1 ? box : 1u, axis == 2 ? box : 1u, 1u};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                               const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
   const CUresult r = reinterpret_cast<Encode>(ctx.encode_tiled)(
       map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, data, dims, strides, boxd, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      cols == 16 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(CYR_ERR_CUDA, "tensor map encoding failed (%d)", int(r));
   return CYR_OK;
 }
@@ -369,6 +372,22 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     RowPassParams rp{data, uint32_t(size_t(ny) * nz * count), tw, ny * nz, nvox};
     const size_t smem = (N + 8 * N) * sizeof(float2);
     k_fft_rows<V><<<(rp.rows + 7) / 8, 256, smem, st>>>(rp);
+  } else if (V == 32 && nx % 8 == 0 && ctx.encode_tiled && ctx.tma_error) {
+    // 1024-point lines: 8-column tiles (k_fft_cols_tma64)
+    CUtensorMap map;
+    CYR_TRY(encode_cols_map(ctx, &map, data, nx, ny, nz, count, nvox, axis, 256, 8));
+    ColTmaParams tp{};
+    tp.nxt = nx / 8;
+    tp.others = axis == 1 ? nz : ny;
+    tp.ntiles = tp.nxt * tp.others * count;
+    tp.axis = uint32_t(axis);
+    tp.tw = tw;
+    tp.error = ctx.tma_error;
+    int sms = 0, per_sm = 0;
+    CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+    CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma64<32>, 9 * 32, cols_tma64_smem(N)));
+    const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
+    k_fft_cols_tma64<32><<<grid, 9 * 32, cols_tma64_smem(N), st>>>(map, tp);
   } else if ((V == 8 || V == 16) && nx % kTmaCols == 0 && ctx.encode_tiled && ctx.tma_error) {
     CUtensorMap map;
     CYR_TRY(encode_cols_map(ctx, &map, data, nx, ny, nz, count, nvox, axis, N < 256 ? N : 256));

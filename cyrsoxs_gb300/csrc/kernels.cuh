@@ -1084,6 +1084,122 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
   }
 }
 
+// 1024-point lines: two 16-column stages do not fit shared memory, so tiles are
+// 8 columns (64-byte lines, 64-byte swizzle: chunk c of line r at
+// c ^ ((r >> 1) & 3)), 8 compute warps of one column each and a producer warp,
+// with the same two-stage protocol as k_fft_cols_tma_ws.
+__host__ __device__ constexpr size_t cols_tma64_smem(uint32_t n) {
+  return 2 * size_t(n) * 8 * 8 + size_t(8) * n * 8 + size_t(n) * 8 + 32 + 1024;
+}
+
+template <int V>
+__global__ void __launch_bounds__(9 * 32, 1) k_fft_cols_tma64(const __grid_constant__ CUtensorMap tmap,
+                                                              ColTmaParams p) {
+  constexpr uint32_t N = 32 * V, TILE = N * 8;  // float2 per tile (8 columns)
+  constexpr uint32_t BOX = 256, NBOX = N / BOX, NW = 8;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  float2 *tiles = reinterpret_cast<float2 *>(base);  // [2][N][8], swizzled
+  float2 *lines = tiles + 2 * TILE;                  // [compute warps][N]
+  float2 *tws = lines + NW * N;                      // [N]
+  uint64_t *full = reinterpret_cast<uint64_t *>(tws + N), *empty = full + 2;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(&empty[0], NW);
+    mbar_init(&empty[1], NW);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  warp_twiddles<V>(tws, p.tw);
+  __syncthreads();
+  // p.nxt counts tiles of 8 columns
+  auto coords = [&](uint32_t t, uint32_t b, int (&c)[4]) {
+    const uint32_t rest = t / p.nxt;
+    c[0] = int((t % p.nxt) * 8);
+    c[3] = int(rest / p.others);
+    if (p.axis == 1) {
+      c[1] = int(b * BOX), c[2] = int(rest % p.others);
+    } else {
+      c[1] = int(rest % p.others), c[2] = int(b * BOX);
+    }
+  };
+  auto region = [&](int s, uint32_t b) { return tiles + s * TILE + b * BOX * 8; };
+  const uint32_t limit = p.poll_limit ? p.poll_limit : kTmaWaitPolls;
+  if (warp == NW) {  // producer
+    if (lane != 0) return;
+    auto store = [&](uint32_t t, int s) {
+#pragma unroll
+      for (uint32_t b = 0; b < NBOX; ++b) {
+        int c[4];
+        coords(t, b, c);
+        tma_store_4d(&tmap, c[0], c[1], c[2], c[3], region(s, b));
+      }
+      bulk_commit();
+    };
+    bool ok = true;
+    uint32_t k = 0;
+    int last[2] = {-1, -1};
+    for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x, ++k) {
+      const int s = int(k & 1u);
+      if (k >= 2) {
+        ok = mbar_wait(&empty[s], ((k >> 1) - 1) & 1u, limit);
+        if (!ok) break;
+        store(t - 2 * gridDim.x, s);
+        bulk_wait_read_all();
+      }
+      mbar_expect_tx(&full[s], TILE * 8 + p.extra_tx);
+      last[s] = int(k);
+#pragma unroll
+      for (uint32_t b = 0; b < NBOX; ++b) {
+        int c[4];
+        coords(t, b, c);
+        tma_load_4d(region(s, b), &tmap, c[0], c[1], c[2], c[3], &full[s]);
+      }
+    }
+    const uint32_t ntile = p.ntiles > blockIdx.x ? (p.ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
+    for (uint32_t kk = ntile >= 2 ? ntile - 2 : 0u; ok && kk < ntile; ++kk) {
+      const int s = int(kk & 1u);
+      ok = mbar_wait(&empty[s], (kk >> 1) & 1u, limit);
+      if (ok) store(blockIdx.x + kk * gridDim.x, s);
+    }
+    if (!ok) {
+      atomicExch(p.error, 1u);
+      for (int st = 0; st < 2; ++st)
+        if (last[st] >= 0) mbar_wait(&full[st], (uint32_t(last[st]) >> 1) & 1u, limit);
+    }
+    bulk_wait_all();
+    return;
+  }
+  // compute warps: warp w owns column w
+  float2 *line = lines + warp * N;
+  const uint32_t half = (warp & 1u) << 3, chunk = warp >> 1;
+  uint32_t k = 0;
+  for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++k) {
+    const int s = int(k & 1u);
+    if (!mbar_wait(&full[s], (k >> 1) & 1u, limit)) {
+      if (lane == 0) atomicExch(p.error, 1u);
+      return;
+    }
+    unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE);
+    float2 a[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const uint32_t r = lane + 32 * i;
+      a[i] = *reinterpret_cast<const float2 *>(tb + r * 64 + ((chunk ^ ((r >> 1) & 3u)) << 4) + half);
+    }
+    warp_fft<V>(a, line, tws, lane);
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const uint32_t r = lane + 32 * i;
+      *reinterpret_cast<float2 *>(tb + r * 64 + ((chunk ^ ((r >> 1) & 3u)) << 4) + half) = a[i];
+    }
+    fence_proxy_async();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+}
+
 // Per-thread register FFT for short strided lines (N = 8..64, powers of two):
 // one thread owns one y or z line, and consecutive threads take consecutive
 // x, so each of a warp's N loads and N stores is one contiguous 256-byte
