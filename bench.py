@@ -18,8 +18,8 @@ detector warp).
   (pinned), host->device copy of the morphology and device->host copy of the
   patterns inside the timed region, wall clock.
 * roofline: per-kernel durations from CUDA events recorded around every
-  launch on its stream during profiled steps; algorithmic bytes per launch as
-  documented in the design doc; peak = measured HBM copy bandwidth.
+  launch on its stream during profiled steps; algorithmic bytes per launch from
+  algorithmic_bytes() below; peak = measured HBM copy bandwidth.
 * cpu_baseline: the FP64 CPU oracle (restatement of the reference's per-angle
   algorithm, OpenMP over all host threads) on a bounded sample (1 energy x 2
   E angles of the same morphology); the same sample checks the engine's
