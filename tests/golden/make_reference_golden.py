@@ -3,11 +3,11 @@ CUDA path (built unmodified by oracle/ref/Makefile into oracle/_ref/) on every
 case of cases.py, in its FP32 (as shipped) and FP64 builds, and runs the NPP
 warp probe on npp_cases.py.
 
-Run on a GPU machine after `make -C oracle/ref REF_SRC=<reference tree>`:
-    python tests/golden/make_reference_golden.py <outdir>
+Run on a machine with a GPU after `make -C oracle/ref REF_SRC=<reference tree>`:
+    python tests/golden/make_reference_golden.py [outdir]
 It writes ref_<case>_fp32.bin / ref_<case>_fp64.bin / npp_warp_out.bin and a
-manifest (reference exit codes, run time, GPU name) into <outdir>; the files
-are then committed under tests/golden/.  The inputs are not stored: cases.py
+manifest (reference exit codes, run time, GPU name) into outdir (default:
+tests/golden/, where the files are committed).  The inputs are not stored: cases.py
 regenerates them from their seeds.
 """
 from __future__ import annotations
@@ -70,4 +70,4 @@ def main(outdir: str) -> int:
 
 
 if __name__ == "__main__":
-    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(REPO, "gpurun_out", "golden")))
+    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else HERE))
