@@ -93,19 +93,27 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
         pend = v;
       ++g;
     };
-    for (uint32_t m = 0; m < p.nmat; ++m) {
-      float sx, sy, sz, pa, pui;
-      director<MORPH>(__ldg(&p.vox[m * p.nvox + i]), sx, sy, sz, pa, pui);
-      const float wa = w * pa;
-      const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
-      T += f0 + f1 + f2 + f6;
-      emit(f0);
-      emit(f1);
-      emit(f2);
-      emit(wa * sx * sy);
-      emit(wa * sx * sz);
-      emit(wa * sy * sz);
-      emit(f6);
+    for (uint32_t m0 = 0; m0 < p.nmat; m0 += 4) {
+      float4 sv[4];  // the loads of up to 4 materials are issued before any is used
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (m0 + u < p.nmat) sv[u] = __ldg(&p.vox[(m0 + u) * p.nvox + i]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (m0 + u >= p.nmat) break;
+        float sx, sy, sz, pa, pui;
+        director<MORPH>(sv[u], sx, sy, sz, pa, pui);
+        const float wa = w * pa;
+        const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
+        T += f0 + f1 + f2 + f6;
+        emit(f0);
+        emit(f1);
+        emit(f2);
+        emit(wa * sx * sy);
+        emit(wa * sx * sz);
+        emit(wa * sy * sz);
+        emit(f6);
+      }
     }
     emit(T);
     if (g & 1u) o[size_t(g >> 1) * p.nvox] = make_float2(pend, 0.f);
