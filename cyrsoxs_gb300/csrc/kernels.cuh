@@ -779,18 +779,25 @@ __global__ void __launch_bounds__(TX * 32, cols_min_blocks(V, TX)) k_fft_cols(Co
 }
 
 // ---------------------------------------------------------------------------
-// Column pass over TMA tiles (y or z axis, lines of 256 or 512 points, nx a
-// multiple of 16).  Persistent blocks of 8 warps walk tiles of 16 adjacent
-// columns x N lines of one (plane or row, volume), double-buffered: the
-// tensor-memory accelerator loads tile k+1 (cp.async.bulk.tensor, completion
-// on an mbarrier) while tile k is transformed, and stores each finished tile
-// back with a bulk tensor store.  The tile lands with the 128-byte swizzle
-// (16-byte chunk c of line r at chunk c ^ (r & 7)), so warp w reads its two
-// columns 2w, 2w+1 as one 16-byte chunk per line, eight lines per
-// quarter-warp on eight distinct chunks: no bank conflicts, and no load/store
-// unit work for the tile copies at all.  Each warp transforms its two columns
-// with the warp FFT through its own exchange line.  (One column per warp, 16
-// warps, measured slower: its 8-byte reads put two lanes on each bank pair.)
+// Column passes over TMA tiles (y or z axis).  Persistent blocks walk tiles
+// of adjacent columns x N lines of one (plane or row, volume),
+// double-buffered: the tensor-memory accelerator loads tile k+1
+// (cp.async.bulk.tensor, completion on an mbarrier) while tile k is
+// transformed, and stores each finished tile back with a bulk tensor store.
+// A 16-column tile lands with the 128-byte swizzle (16-byte chunk c of line r
+// at chunk c ^ (r & 7)), so a warp reads its two columns 2w, 2w+1 as one
+// 16-byte chunk per line, eight lines per quarter-warp on eight distinct
+// chunks: no bank conflicts, and no load/store unit work for the tile copies
+// at all.  Each warp transforms its columns with the warp FFT through its own
+// exchange line.  Three forms:
+//  * k_fft_cols_tma: 8 warps, thread 0 issues the copies between tiles
+//    (256-point lines with nx a multiple of 16 but not of 32);
+//  * k_fft_cols_tma_ws<V, H>: H 16-column halves per tile, 8 H compute warps
+//    and a producer warp (512 points: H = 1; 256 points: H = 2);
+//  * k_fft_cols_tma64: 8-column tiles with the 64-byte swizzle for
+//    1024-point lines, one column per warp.
+// (One column per warp on 16-column tiles measured slower: its 8-byte reads
+// put two lanes on each bank pair.)
 // ---------------------------------------------------------------------------
 constexpr int kTmaCols = 16;       // columns per tile (128 bytes per line)
 constexpr int kTmaWarps = kTmaCols / 2;
