@@ -912,12 +912,13 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
     pl.fields = o->strategy == CYR_STRATEGY_FIELDS;
   }
   {
-    // energies per Ewald / rotation launch: their Gram records (LAB) or
-    // per-angle images (MATERIAL) stay within L2 for the rotation; batches of
-    // even size, each a whole number of records
-    const uint32_t nep = gram_nep(pl), cap = std::min<uint32_t>(pl.ne, 32);
+    // energies per Ewald / rotation launch: up to 64, and 256 MB of Gram records
+    // (LAB) or per-angle images (MATERIAL) per batch (fewer, larger launches;
+    // the rotation's reads mostly hit L1, so L2 residency of a batch matters
+    // little); batches of even size, each a whole number of records
+    const uint32_t nep = gram_nep(pl), cap = std::min<uint32_t>(pl.ne, 64);
     uint32_t emax = 1;
-    while (emax < cap && image_bytes(pl, emax + 1) <= (size_t(96) << 20)) ++emax;
+    while (emax < cap && image_bytes(pl, emax + 1) <= (size_t(256) << 20)) ++emax;
     const uint32_t nbatches = (pl.ne + emax - 1) / emax;
     const uint32_t eb = (pl.ne + nbatches - 1) / nbatches;
     pl.ebatch = nbatches == 1 ? pl.ne : std::min(pl.ne, (eb + nep - 1) / nep * nep);
