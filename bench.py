@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--energies-per-step", type=int, default=ENERGIES_PER_STEP)
     ap.add_argument("--strategy", type=int, default=0, choices=[0, 1, 2],
                     help="0 auto, 1 per-energy spectra, 2 field spectra once per request")
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-served", action="store_true", help="skip the batched and serving measurements")
     ap.add_argument("--served-only", action="store_true", help="only the batched and serving measurements")
