@@ -41,6 +41,12 @@ def test_header_declares_the_boundary():
         assert want in names
 
 
+def test_integration_guide_covers_every_declared_symbol():
+    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [n for n in declared_functions() if n not in guide]
+    assert not missing, missing
+
+
 def test_library_exports_every_declared_symbol():
     nat = _native()
     L = ctypes.CDLL(nat.library_path())
