@@ -248,3 +248,35 @@ def reference_reads_in_bounds(case: Case, margin: float = 1e-2) -> bool:
                 if reads.any() and (hi[reads] + 1).max() > case.nz - 1:
                     return False
     return True
+
+
+# ---- isotropic morphologies: the analytical properties of the Born path ----
+# With S = 0 every material is isotropic (phi_a = 0, include/uniaxial.h:58-169),
+# and with n_par = n_perp = n the tensor Nr - phi I is vf (n^2 - 1) I, so the
+# induced polarization is p = sum_m vf_m (n_m^2 - 1) E / 4 pi.  Two exact
+# consequences, checked on the oracle and on the engine:
+#  * scaling every (n_m^2 - 1) by one complex c scales every pattern by |c|^2;
+#  * adding one constant C to every n_m^2 adds C (sum_m vf_m) E / 4 pi, which
+#    for volume fractions summing to 1 is a constant field: it reaches only the
+#    q = 0 bin, and the DC replacement (src/cudaMain.cu:123-176) overwrites that
+#    bin from its neighbours, so the patterns do not change.
+
+def isotropic_voxels(case: Case) -> np.ndarray:
+    """The case's volume fractions with S = theta = psi = 0 (Euler layout)."""
+    vf = _vfrac(case, np.random.Generator(np.random.PCG64(case.seed)))
+    out = np.zeros((case.num_material, case.nz, case.ny, case.nx, 4), np.float32)
+    out[..., 3] = vf
+    return out
+
+
+def constants_from_n2(n2: np.ndarray) -> np.ndarray:
+    """[E][M] complex n^2 -> [E][M][4] float32 (delta, beta) with n_par = n_perp = sqrt(n^2)."""
+    n = np.sqrt(np.asarray(n2, np.complex128))
+    d, b = 1.0 - n.real, n.imag
+    return np.stack([d, b, d, b], -1).astype(np.float32)
+
+
+def n2_from_constants(optical: np.ndarray) -> np.ndarray:
+    """[E][M][4] -> [E][M] complex n^2 of the parallel constants (n = 1 - delta + i beta)."""
+    o = np.asarray(optical, np.float64)
+    return (1.0 - o[..., 0] + 1j * o[..., 1]) ** 2
