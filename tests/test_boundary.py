@@ -94,6 +94,47 @@ def test_invalid_options_are_rejected_before_any_device_work():
     assert ei.value.code == 2
 
 
+GOOD = dict(nx=16, ny=16, nz=8, num_material=2, energies=[285.0], start_angle=0.0, end_angle=90.0,
+            increment_angle=30.0, phys_size=5.0)
+
+
+@pytest.mark.parametrize("over,code,words", [
+    (dict(nx=1), 1, "dimensions"),
+    (dict(ny=1), 1, "dimensions"),
+    (dict(nz=0), 1, "dimensions"),
+    (dict(num_material=0), 1, "num_material"),
+    (dict(num_material=33), 1, "num_material"),
+    (dict(energies=[]), 1, "no energies"),
+    (dict(energies=[285.0, 0.0]), 1, "energies must be positive"),
+    (dict(energies=[float("nan")]), 1, "energies must be positive"),
+    (dict(phys_size=0.0), 1, "phys_size"),
+    (dict(phys_size=float("nan")), 1, "phys_size"),
+    (dict(case_type=3), 1, "case_type"),
+    (dict(ewald_interpolation=2), 1, "enumerated"),
+    (dict(reference_frame=2), 1, "enumerated"),
+    (dict(strategy=3), 1, "enumerated"),
+    (dict(start_angle=90.0, end_angle=0.0), 1, "start angle"),
+    (dict(increment_angle=0.0), 1, "increment angle is 0"),
+    (dict(end_angle=4096.0, increment_angle=0.5), 1, "angle count"),
+    (dict(nz=13), 2, "prime factor"),
+    (dict(nx=6561, ny=2, nz=1), 2, "single-block FFT limit"),  # 3^8: factorable, above one block
+], ids=lambda v: str(v) if not isinstance(v, dict) else ",".join(f"{k}={w}" for k, w in v.items()))
+def test_each_invalid_option_is_rejected_with_its_reason(over, code, words):
+    nat = _native()
+    with pytest.raises(nat.CyrError) as ei:
+        nat.required_device_bytes(nat.Options(**{**GOOD, **over}))
+    assert ei.value.code == code
+    assert words in str(ei.value)
+
+
+def test_edge_shapes_that_are_valid_plan_on_the_host():
+    nat = _native()
+    for over in (dict(nz=1), dict(nx=2, ny=2, nz=1), dict(num_material=32), dict(start_angle=30.0, end_angle=30.0,
+                                                                                   increment_angle=0.0),
+                 dict(nx=7, ny=5, nz=3), dict(end_angle=4095.0, increment_angle=1.0)):
+        assert nat.required_device_bytes(nat.Options(**{**GOOD, **over})) > 0
+
+
 def test_required_bytes_counts_the_tensor_volumes():
     nat = _native()
     opts = nat.Options(nx=64, ny=64, nz=16, num_material=2, energies=[280.0, 285.0], start_angle=0, end_angle=165,
