@@ -168,6 +168,40 @@ def make_input(M=2, dims=(4, 8, 6), order=None):
     return inp
 
 
+REF_PYMAIN = "/root/reference/src/pymain.cpp"
+
+
+@pytest.mark.skipif(not os.path.isfile(REF_PYMAIN), reason="the reference's pybind11 module source is not here")
+def test_module_exposes_every_name_the_reference_binds():
+    """Every class, enum value, method and property src/pymain.cpp binds exists in the drop-in."""
+    c = cy()
+    src = open(REF_PYMAIN).read()
+    instances = {"InputData": lambda: c.InputData(NumMaterial=2)}
+    missing, seen = [], 0
+    for block in re.split(r"(?=py::(?:class_|enum_)<)", src)[1:]:
+        m = re.match(r'py::(?:class_|enum_)<[^>]*>\s*\(\s*\w+\s*,\s*"(\w+)"', block)
+        if not m:
+            continue
+        name = m.group(1)
+        body = block[:block.find(";")]
+        members = re.findall(r'\.def(?:_readwrite|_readonly|_property\w*)?\(\s*"(\w+)"', body)
+        members += re.findall(r'\.value\(\s*"(\w+)"', body)
+        obj = getattr(c, name, None)
+        if obj is None:
+            missing.append(name)
+            continue
+        inst = instances[name]() if name in instances else None
+        for n in members:
+            seen += 1
+            if not hasattr(obj, n) and not (inst is not None and hasattr(inst, n)):
+                missing.append(f"{name}.{n}")
+    for n in re.findall(r'\b(?:m|module)\.def\(\s*"(\w+)"', src):
+        seen += 1
+        if not hasattr(c, n):
+            missing.append(n)
+    assert seen > 50 and not missing, missing
+
+
 def test_input_data_setters_follow_the_reference(capsys):
     c = cy()
     inp = make_input()
