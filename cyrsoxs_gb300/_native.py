@@ -102,8 +102,38 @@ def check(rc: int) -> None:
 
 
 def fptr(a: np.ndarray):
-    assert a.dtype == np.float32 and a.flags.c_contiguous
+    if not isinstance(a, np.ndarray) or a.dtype != np.float32 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float32 numpy array")
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def expect_size(a: np.ndarray, n: int, what: str) -> np.ndarray:
+    """a as C-contiguous float32 with exactly n elements: the engine reads or writes that many."""
+    if not isinstance(a, np.ndarray) or a.dtype != np.float32 or not a.flags.c_contiguous:
+        raise TypeError(f"{what} must be a C-contiguous float32 numpy array")
+    if a.size != n:
+        raise ValueError(f"{what} has {a.size} elements; these options need {n}")
+    return a
+
+
+def optical_array(opts: "Options", optical) -> np.ndarray:
+    s = opts.struct
+    return expect_size(np.ascontiguousarray(optical, np.float32), s.num_energies * s.num_material * 4,
+                       "optical constants [E][M][4]")
+
+
+def voxel_count(opts: "Options") -> int:
+    s = opts.struct
+    return s.num_material * s.nz * s.ny * s.nx * 4
+
+
+def voxel_array(opts: "Options", voxels) -> np.ndarray:
+    return expect_size(np.ascontiguousarray(voxels, np.float32), voxel_count(opts), "voxels [M][Z][Y][X][4]")
+
+
+def pattern_count(opts: "Options") -> int:
+    s = opts.struct
+    return s.num_energies * opts.num_k * s.ny * s.nx
 
 
 class Options:
@@ -154,10 +184,10 @@ def cuda_main(opts: Options, optical: np.ndarray, voxels: np.ndarray, streams_va
     shape = (s.num_energies, opts.num_k, s.ny, s.nx)
     if out is None:
         out = np.empty(shape, np.float32)
-    assert out.shape == shape and out.dtype == np.float32 and out.flags.c_contiguous
+    expect_size(out, pattern_count(opts), "out [E][K][Ny][Nx]")
+    opt_arr, vox = optical_array(opts, optical), voxel_array(opts, voxels)
     fn = lib().cyr_cuda_main_streams if streams_variant else lib().cyr_cuda_main
-    check(fn(opts.ref, fptr(np.ascontiguousarray(optical, np.float32)), fptr(np.ascontiguousarray(voxels, np.float32)),
-             fptr(out)))
+    check(fn(opts.ref, fptr(opt_arr), fptr(vox), fptr(out)))
     return out
 
 
@@ -166,9 +196,9 @@ def compute_polarization(opts: Options, optical, voxels, eangle: float, energy_i
     shape = (s.nz, s.ny, s.nx)
     px, py, pz = (np.empty(shape, np.complex64) for _ in range(3))
     as_f = lambda a: a.view(np.float32)  # noqa: E731
-    check(lib().cyr_compute_polarization(opts.ref, fptr(np.ascontiguousarray(optical, np.float32)),
-                                         fptr(np.ascontiguousarray(voxels, np.float32)), float(eangle), int(energy_id),
-                                         fptr(as_f(px)), fptr(as_f(py)), fptr(as_f(pz))))
+    check(lib().cyr_compute_polarization(opts.ref, fptr(optical_array(opts, optical)), fptr(voxel_array(opts, voxels)),
+                                         float(eangle), int(energy_id), fptr(as_f(px)), fptr(as_f(py)),
+                                         fptr(as_f(pz))))
     return px, py, pz
 
 
@@ -179,7 +209,7 @@ def required_device_bytes(opts: Options) -> int:
 
 
 def simulate_device(opts: Options, optical: np.ndarray, d_voxels: int, d_out: int, stream: int = 0) -> None:
-    check(lib().cyr_simulate_device(opts.ref, fptr(np.ascontiguousarray(optical, np.float32)), ctypes.c_void_p(d_voxels),
+    check(lib().cyr_simulate_device(opts.ref, fptr(optical_array(opts, optical)), ctypes.c_void_p(d_voxels),
                                     ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
 
 

@@ -49,13 +49,14 @@ class Server:
         self._keep = {}  # id -> objects the request reads or writes until it is done
 
     def submit(self, opts: _native.Options, optical: np.ndarray, voxels, out, device: bool = False) -> int:
-        opt_arr = np.ascontiguousarray(optical, np.float32)
+        opt_arr = _native.optical_array(opts, optical)
         if device:
             vptr, optr = ctypes.c_void_p(int(voxels)), ctypes.c_void_p(int(out))
             keep = (opts, opt_arr)
         else:
-            assert voxels.dtype == np.float32 and voxels.flags.c_contiguous
-            assert out.dtype == np.float32 and out.flags.c_contiguous
+            # the engine reads and writes these in place until the request is done: no copies
+            _native.expect_size(voxels, _native.voxel_count(opts), "voxels [M][Z][Y][X][4]")
+            _native.expect_size(out, _native.pattern_count(opts), "out [E][K][Ny][Nx]")
             vptr, optr = ctypes.c_void_p(voxels.ctypes.data), ctypes.c_void_p(out.ctypes.data)
             keep = (opts, opt_arr, voxels, out)
         rid = ctypes.c_uint64()

@@ -80,6 +80,33 @@ def test_without_gpu_the_engine_fails_loudly():
     assert ei.value.code == 5  # CYR_ERR_NO_DEVICE
 
 
+def test_host_arrays_of_the_wrong_size_or_type_are_refused_before_the_engine_reads_them():
+    nat = _native()
+    opts = nat.Options(nx=8, ny=8, nz=4, num_material=2, energies=[285.0, 286.0], start_angle=0, end_angle=0,
+                       increment_angle=0, phys_size=5.0)
+    opt = np.zeros((2, 2, 4), np.float32)
+    vox = np.zeros((2, 4, 8, 8, 4), np.float32)
+    with pytest.raises(ValueError, match="optical constants"):
+        nat.cuda_main(opts, opt[:1], vox)
+    with pytest.raises(ValueError, match="voxels"):
+        nat.cuda_main(opts, opt, vox[:1])
+    with pytest.raises(ValueError, match="out"):
+        nat.cuda_main(opts, opt, vox, out=np.zeros((1, 1, 8, 8), np.float32))
+    with pytest.raises(TypeError, match="out"):
+        nat.cuda_main(opts, opt, vox, out=np.zeros((2, 1, 8, 8), np.float64))
+    with pytest.raises(TypeError, match="out"):
+        nat.cuda_main(opts, opt, vox, out=np.zeros((2, 1, 8, 16), np.float32)[..., ::2])
+    with pytest.raises(ValueError, match="voxels"):
+        nat.compute_polarization(opts, opt, vox[:, :2], 0.0, 0)
+    with pytest.raises(ValueError, match="optical constants"):
+        nat.simulate_device(opts, opt[:, :1], 0, 0)
+    # other dtypes and layouts of the inputs are converted, not refused
+    if nat.device_count() == 0:
+        with pytest.raises(nat.CyrError) as ei:
+            nat.cuda_main(opts, opt.astype(np.float64), np.asfortranarray(vox))
+        assert ei.value.code == 5
+
+
 def test_invalid_options_are_rejected_before_any_device_work():
     nat = _native()
     opts = nat.Options(nx=8, ny=8, nz=4, num_material=1, energies=[285.0], start_angle=10, end_angle=0,
