@@ -71,7 +71,7 @@ def run(morphology_file: str, out_dir: str | None = None, config_file: str = "co
         return 1
     try:
         out = _native.cuda_main(inp._options(), optical, morph.voxels, streams_variant=inp.algorithmType == 1)
-    except _native.CyrError as exc:
+    except (_native.CyrError, ValueError, TypeError) as exc:
         print(exc)
         return 1
     h5io.write_scattering(inp, out, cfg["HDF5DirName"])
