@@ -92,6 +92,7 @@ def lib():
     L.cyr_stage_name.argtypes = [ctypes.c_uint32]
     L.cyr_stage_name.restype = ctypes.c_char_p
     L.cyr_num_stages.restype = ctypes.c_uint32
+    L.cyr_release_scratch.argtypes = []
     _lib = L
     return L
 
@@ -271,6 +272,11 @@ def profile_end():
         if launches[i]:
             out[lib().cyr_stage_name(i).decode()] = (int(launches[i]), float(ms[i]), int(calls[i]))
     return out, int(dropped.value)
+
+
+def release_scratch() -> None:
+    """Frees the library's cached scratch space on the current device (cyr_release_scratch)."""
+    check(lib().cyr_release_scratch())
 
 
 def device_count() -> int:

@@ -100,6 +100,9 @@ bool factorize(uint32_t n, std::vector<uint32_t> &radix) {
 
 constexpr size_t kFftSmemBudget = 200 * 1024;
 
+// The FFT kernels address elements inside one volume with 32-bit offsets.
+constexpr size_t kMaxVolumeVoxels = 0xffffffffull;
+
 // Lines per block: about 4096 elements per tile, at most 16 lines.
 uint32_t fft_lines_per_block(uint32_t n) {
   uint32_t tx = 16;
@@ -735,6 +738,9 @@ int validate(const cyr_options *o) {
     return fail(CYR_ERR_ARGUMENT, "increment angle is 0");
   for (uint32_t e = 0; e < o->num_energies; ++e)
     if (!(o->energies[e] > 0)) return fail(CYR_ERR_ARGUMENT, "energies must be positive");
+  if (size_t(o->nx) * o->ny * o->nz > kMaxVolumeVoxels)
+    return fail(CYR_ERR_UNSUPPORTED, "volume of %u x %u x %u voxels exceeds the limit of 2^32 - 1 voxels", o->nx, o->ny,
+                o->nz);
   std::vector<uint32_t> r;
   const uint32_t d[3] = {o->nx, o->ny, o->nz};
   for (uint32_t n : d)
@@ -2180,6 +2186,8 @@ uint32_t cyr_num_stages(void) { return kNumStages; }
 
 int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, void *stream) {
   if (!d_data || nx < 1 || ny < 1 || nz < 1 || count < 1) return fail(CYR_ERR_ARGUMENT, "bad FFT arguments");
+  if (size_t(nx) * ny * nz > kMaxVolumeVoxels)
+    return fail(CYR_ERR_ARGUMENT, "volume of %u x %u x %u elements exceeds the limit of 2^32 - 1", nx, ny, nz);
   std::vector<uint32_t> r;
   for (uint32_t n : {nx, ny, nz})
     if (n > 1 && !factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u has a prime factor above 7", n);
@@ -2227,8 +2235,10 @@ int cyr_selftest_wait_limit(int *timed_out) {
       rc = fail(CYR_ERR_CUDA, "self-test kernel failed: %s", cudaGetErrorString(e));
       break;
     }
-    *timed_out = flag != 0;
+    *timed_out = (flag & 1u) != 0;
     if (cudaMemset(ctx->tma_error, 0, sizeof(unsigned)) != cudaSuccess) rc = fail(CYR_ERR_CUDA, "flag reset failed");
+    if ((flag & 2u) != 0)
+      rc = fail(CYR_ERR_TIMEOUT, "the copies of the timed-out tile did not land within the drain's wait limit");
   } while (false);
   cudaFree(d);
   return rc;
@@ -2392,6 +2402,7 @@ namespace {
 constexpr uint32_t kStaticMaxLength = 4096;  // per axis
 constexpr size_t kStaticTwiddleBytes = size_t(3) * kStaticMaxLength * sizeof(float2);  // 96 KiB
 __device__ __align__(256) float2 g_static_twiddles[3 * kStaticMaxLength];
+static_assert(sizeof(g_static_twiddles) == kStaticTwiddleBytes, "static twiddle array size");
 
 struct StaticTwiddleState {
   float2 *dev_ptr = nullptr;  // device address of g_static_twiddles on this device
@@ -2401,12 +2412,26 @@ std::mutex g_static_mu;
 std::map<int, StaticTwiddleState> g_static_state;
 }  // namespace
 
+// W_n^m = exp(-2 pi i m / n) for the three axes, formed with sincospi in double
+// and rounded to float; axis a's table starts at a * kStaticMaxLength.
+__global__ void k_static_twiddles(float2 *tab, uint32_t nx, uint32_t ny, uint32_t nz) {
+  const uint32_t axis = blockIdx.y;
+  const uint32_t n = axis == 0 ? nx : axis == 1 ? ny : nz;
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+    double sn, cs;
+    sincospi(-2.0 * double(m) / double(n), &sn, &cs);
+    tab[size_t(axis) * kStaticMaxLength + m] = make_float2(float(cs), float(sn));
+  }
+}
+
 extern "C" int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count,
                                        void *stream) {
   if (!d_data || nx < 1 || ny < 1 || nz < 1 || count < 1) return fail(CYR_ERR_ARGUMENT, "bad FFT arguments");
   if (nx > kStaticMaxLength || ny > kStaticMaxLength || nz > kStaticMaxLength)
     return fail(CYR_ERR_ARGUMENT, "cyr_fft3d_device_static: every axis must be at most %u long (got %u x %u x %u)",
                 kStaticMaxLength, nx, ny, nz);
+  if (size_t(nx) * ny * nz > kMaxVolumeVoxels)
+    return fail(CYR_ERR_ARGUMENT, "volume of %u x %u x %u elements exceeds the limit of 2^32 - 1", nx, ny, nz);
   if (count > 65535) return fail(CYR_ERR_ARGUMENT, "too many volumes in one call");
   std::vector<uint32_t> r;
   for (uint32_t n : {nx, ny, nz})
@@ -2423,30 +2448,21 @@ extern "C" int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, u
     stt.dev_ptr = static_cast<float2 *>(p);
   }
   if (!stt.attrs) {
+    // the only kernel this entry point launches with large dynamic shared memory
     const int smem = int(kFftSmemBudget);
     CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CYR_CUDA(cudaFuncSetAttribute(k_fft_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-#define CYR_COLS_ATTR(V, T) \
-  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  CYR_COLS_ATTR(4, kColsTxY) CYR_COLS_ATTR(8, kColsTxY) CYR_COLS_ATTR(16, kColsTxY)
-  CYR_COLS_ATTR(4, kColsTxZ) CYR_COLS_ATTR(8, kColsTxZ) CYR_COLS_ATTR(16, kColsTxZ)
-#undef CYR_COLS_ATTR
     stt.attrs = true;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // The tables of this call replace the previous call's contents (every entry
-  // the passes read is written here, nothing relies on zeros).  Calls whose
-  // work overlaps on the GPU share the array and race.
+  // The tables of this call replace the previous call's contents: a kernel on
+  // `st` writes every entry the passes read, so nothing relies on zeros and no
+  // host copy is involved.  Calls whose work overlaps on the GPU share the
+  // array and race.
+  k_static_twiddles<<<dim3(16, 3), 256, 0, st>>>(stt.dev_ptr, nx, ny, nz);
+  CYR_CUDA(cudaGetLastError());
   const uint32_t dims[3] = {nx, ny, nz};
-  std::vector<float2> host(size_t(3) * kStaticMaxLength);
-  for (int a = 0; a < 3; ++a)
-    for (uint32_t m = 0; m < dims[a]; ++m) {
-      const double ang = -2.0 * kPi * double(m) / double(dims[a]);
-      host[size_t(a) * kStaticMaxLength + m] = make_float2(float(std::cos(ang)), float(std::sin(ang)));
-    }
-  // pageable source: the copy is staged before this call returns
-  CYR_CUDA(cudaMemcpyAsync(stt.dev_ptr, host.data(), kStaticTwiddleBytes, cudaMemcpyHostToDevice, st));
   const size_t nvox = size_t(nx) * ny * nz;
   for (int axis = 0; axis < 3; ++axis) {
     const uint32_t n = dims[axis];

@@ -808,7 +808,8 @@ struct ColTmaParams {
   uint32_t others;   // y pass: planes per volume; z pass: rows (ny)
   uint32_t axis;     // 1: lines along y (tensor dim 1), 2: along z (dim 2)
   const float2 *tw;  // twiddles of length N
-  unsigned *error;   // set to 1 when a tile copy did not complete within the wait limit
+  unsigned *error;   // bit 1: a tile copy did not complete within the wait limit; bit 2: the drain
+                     // after that timeout did not see the block's issued copies land either
   // self-test of the bounded waits (cyr_selftest_wait_limit); 0 in normal use:
   uint32_t poll_limit;  // polls per wait (0: kTmaWaitPolls)
   uint32_t extra_tx;    // bytes expected beyond the tile's, so its phase never completes
@@ -830,6 +831,20 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
 }
+// Completes `bytes` of the current phase's expected transaction count without a
+// copy.  Only the wait-limit self-test needs it: its loads deliver extra_tx
+// bytes fewer than the barrier expects, and after the timeout the producer
+// completes those bytes itself, so that its drain wait ends exactly when the
+// copies it really issued have landed.
+__device__ __forceinline__ void mbar_complete_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.complete_tx.relaxed.cta.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// After a timeout: waits (bounded) for the last phase issued on a stage, so
+// the block does not release shared memory under copies still landing; sets
+// bit 2 of the error word if even that wait runs out.
+__device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity, uint32_t limit, uint32_t extra_tx,
+                                           unsigned *error);
 // Waits for the phase with the given parity; false if it did not complete within `limit` polls.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
   const uint32_t a = smem_u32(bar);
@@ -843,6 +858,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
     if (done) return true;
   }
   return false;
+}
+__device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity, uint32_t limit, uint32_t extra_tx,
+                                           unsigned *error) {
+  if (extra_tx) mbar_complete_tx(bar, extra_tx);
+  if (!mbar_wait(bar, parity, limit)) atomicOr(error, 2u);
 }
 __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
                                             uint64_t *bar) {
@@ -917,10 +937,10 @@ __global__ void __launch_bounds__(kTmaWarps * 32, 1) k_fft_cols_tma(const __grid
     const bool ok = mbar_wait(&mbar[s], (k >> 1) & 1u, limit);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
-        atomicExch(p.error, 1u);
+        atomicOr(p.error, 1u);
         // let the copies in flight land (bounded) before the block releases its shared memory
-        mbar_wait(&mbar[s], (k >> 1) & 1u, limit);
-        if (t + gridDim.x < p.ntiles) mbar_wait(&mbar[s ^ 1], ((k + 1) >> 1) & 1u, limit);
+        mbar_drain(&mbar[s], (k >> 1) & 1u, limit, p.extra_tx, p.error);
+        if (t + gridDim.x < p.ntiles) mbar_drain(&mbar[s ^ 1], ((k + 1) >> 1) & 1u, limit, p.extra_tx, p.error);
       }
       break;
     }
@@ -1049,10 +1069,10 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
       if (ok) store(blockIdx.x + kk * gridDim.x, s);
     }
     if (!ok) {
-      atomicExch(p.error, 1u);
+      atomicOr(p.error, 1u);
       // the block must not release its shared memory under copies still landing
       for (int st = 0; st < 2; ++st)
-        if (last[st] >= 0) mbar_wait(&full[st], (uint32_t(last[st]) >> 1) & 1u, limit);
+        if (last[st] >= 0) mbar_drain(&full[st], (uint32_t(last[st]) >> 1) & 1u, limit, p.extra_tx, p.error);
     }
     bulk_wait_all();
     return;
@@ -1065,7 +1085,7 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
   for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++k) {
     const int s = int(k & 1u);
     if (!mbar_wait(&full[s], (k >> 1) & 1u, limit)) {
-      if (lane == 0) atomicExch(p.error, 1u);
+      if (lane == 0) atomicOr(p.error, 1u);
       return;
     }
     unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE + hw * HALF);
@@ -1171,9 +1191,9 @@ __global__ void __launch_bounds__(9 * 32, 1) k_fft_cols_tma64(const __grid_const
       if (ok) store(blockIdx.x + kk * gridDim.x, s);
     }
     if (!ok) {
-      atomicExch(p.error, 1u);
+      atomicOr(p.error, 1u);
       for (int st = 0; st < 2; ++st)
-        if (last[st] >= 0) mbar_wait(&full[st], (uint32_t(last[st]) >> 1) & 1u, limit);
+        if (last[st] >= 0) mbar_drain(&full[st], (uint32_t(last[st]) >> 1) & 1u, limit, p.extra_tx, p.error);
     }
     bulk_wait_all();
     return;
@@ -1185,7 +1205,7 @@ __global__ void __launch_bounds__(9 * 32, 1) k_fft_cols_tma64(const __grid_const
   for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++k) {
     const int s = int(k & 1u);
     if (!mbar_wait(&full[s], (k >> 1) & 1u, limit)) {
-      if (lane == 0) atomicExch(p.error, 1u);
+      if (lane == 0) atomicOr(p.error, 1u);
       return;
     }
     unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE);

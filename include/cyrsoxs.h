@@ -153,7 +153,8 @@ CYR_API int cyr_release_scratch(void);
  *
  * cyr_fft3d_device: in-place forward unnormalised 3D DFT of `count`
  * consecutive complex [nz][ny][nx] volumes (cufftExecC2C FORWARD semantics,
- * include/cudaMain.h:184-190).
+ * include/cudaMain.h:184-190).  One volume may hold at most 2^32 - 1
+ * elements (larger volumes are refused with CYR_ERR_ARGUMENT).
  */
 CYR_API int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, void *stream);
 
@@ -165,11 +166,13 @@ CYR_API int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz
  * or allocating library routine: its twiddle tables live in a fixed 96 KiB
  * device array that is part of the library image and that every GPU loading
  * the library holds until the process exits.  Each axis may be at most 4096
- * long; longer axes are rejected with CYR_ERR_ARGUMENT.  The first call on a
- * device resolves the array's device address (cudaGetSymbolAddress), so make
- * that first call before any stream capture.  All calls share the array and
- * each call rewrites it: calls whose work overlaps on the GPU race.
- * This entry point has no counterpart in the reference.
+ * long, and one volume at most 2^32 - 1 elements; larger sizes are rejected
+ * with CYR_ERR_ARGUMENT.  The first call on a device resolves the array's
+ * device address (cudaGetSymbolAddress) and sets the FFT kernel's
+ * shared-memory limit, so make that first call before any stream capture.
+ * Every call recomputes the tables in the array with a kernel on `stream`
+ * (no host copy).  All calls share the array: calls whose work overlaps on
+ * the GPU race.  This entry point has no counterpart in the reference.
  */
 CYR_API int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count,
                                     void *stream);
@@ -178,8 +181,10 @@ CYR_API int cyr_fft3d_device_static(void *d_data, uint32_t nx, uint32_t ny, uint
  * cyr_selftest_wait_limit: checks the bounded waits of the TMA column FFT pass.
  * It runs that kernel once on a 32 x 256 tile whose copies deliver fewer bytes
  * than the kernel's barrier expects, so every wait runs out; the kernel must
- * report it (*timed_out = 1), wait for its copies, and leave the context
- * usable.  Synchronises the device.  No counterpart in the reference.
+ * report it (*timed_out = 1), wait for the copies it issued, and leave the
+ * context usable.  Returns CYR_ERR_TIMEOUT if the kernel could not confirm
+ * within its wait limit that those copies landed.  Synchronises the device.
+ * No counterpart in the reference.
  */
 CYR_API int cyr_selftest_wait_limit(int *timed_out);
 

@@ -6,8 +6,9 @@ import numpy as np
 import pytest
 
 from cyrsoxs_gb300 import cli, config, h5io
+from reference_tree import reference_file
 
-REF_DATA = "/root/reference/Data"
+REF_DATA = reference_file("Data")
 
 CONFIG = """# a comment
 CaseType = 1;
@@ -68,7 +69,7 @@ def test_read_materials(tmp_path):
         config.read_materials(2, [285.0, 281.0], str(tmp_path))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_DATA), reason="the reference's example inputs are not here")
+@pytest.mark.skipif(REF_DATA is None, reason="the reference's example inputs are not here")
 def test_reads_the_reference_example_inputs():
     c = config.read_config(os.path.join(REF_DATA, "config.txt"))
     assert c["energies"] == [280.0] and c["morphologyType"] == 1

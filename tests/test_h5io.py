@@ -7,8 +7,9 @@ import numpy as np
 import pytest
 
 from cyrsoxs_gb300 import h5io
+from reference_tree import reference_file
 
-REF_FIXTURE = "/root/reference/Data/edgeSphereZYX.h5"
+REF_FIXTURE = reference_file("Data", "edgeSphereZYX.h5")
 
 
 def test_round_trip_datasets_groups_and_labels(tmp_path):
@@ -99,7 +100,7 @@ def test_drop_in_read_from_h5(tmp_path, capsys):
     assert "PhysSize mismatch" in capsys.readouterr().out
 
 
-@pytest.mark.skipif(not os.path.exists(REF_FIXTURE), reason="the reference's example morphology is not here")
+@pytest.mark.skipif(REF_FIXTURE is None, reason="the reference's example morphology is not here")
 def test_reads_the_reference_example_morphology():
     m = h5io.read_morphology(REF_FIXTURE, 1)  # vector morphology, ZYX
     assert m.num_material == 2 and m.phys_size == 5.0 and m.order == 0 and m.dims_xyz == (32, 32, 16)

@@ -8,8 +8,10 @@ in a fixed device array instead of allocating them.  This test calls that
 entry point through the C ABI and checks it against the allocating entry
 point, cyr_fft3d_device, on two calls in a row with different shapes.  Each
 call rewrites the shared array, so the second call must not see the first
-call's tables.  It also checks that axes longer than the array's limit are
-refused.
+call's tables; the x length also changes and comes back (48, 64, 48), so
+stale entries left in the array by a longer axis would show.  The shapes
+reach the entry point's limit of 4096 points along x, y and z.  It also
+checks that axes longer than the array's limit are refused.
 
 The file is named so that pytest collects it last.  It needs no other test and
 passes when run alone.
@@ -47,13 +49,29 @@ def _run_both(torch, nat, shape, count, seed):
     return got, want, ref
 
 
+def _check(got, want, ref):
+    scale = np.abs(want).max()
+    assert np.abs(got - want).max() <= TOL * scale
+    assert np.abs(got.astype(np.complex128) - ref).max() <= TOL * np.abs(ref).max()
+
+
 def test_static_fft_matches_allocating_fft_on_two_calls_in_a_row():
     torch, nat = _setup()
     for shape, count, seed in (((16, 32, 48), 2, 1), ((7, 20, 64), 3, 2)):
-        got, want, ref = _run_both(torch, nat, shape, count, seed)
-        scale = np.abs(want).max()
-        assert np.abs(got - want).max() <= TOL * scale
-        assert np.abs(got.astype(np.complex128) - ref).max() <= TOL * np.abs(ref).max()
+        _check(*_run_both(torch, nat, shape, count, seed))
+
+
+def test_static_fft_when_an_axis_length_changes_between_calls():
+    torch, nat = _setup()
+    for i, nx in enumerate((48, 64, 48)):
+        _check(*_run_both(torch, nat, (6, 10, nx), 2, 10 + i))
+
+
+@pytest.mark.parametrize("shape,count", [((2, 256, 4096), 1), ((4, 1000, 512), 1), ((3, 2048, 7), 2),
+                                         ((8, 4096, 3), 1), ((4096, 2, 8), 1)])
+def test_static_fft_long_axes_up_to_its_limit(shape, count):
+    torch, nat = _setup()
+    _check(*_run_both(torch, nat, shape, count, sum(shape)))
 
 
 def test_static_fft_refuses_axes_beyond_its_limit():
