@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-served", action="store_true", help="skip the batched and serving measurements")
+    ap.add_argument("--skip-reference-gpu", action="store_true",
+                    help="skip timing the reference's own GPU build beside the engine")
+    ap.add_argument("--skip-c4", action="store_true", help="skip the 256 x 1024 x 1024 precision sample")
     ap.add_argument("--served-only", action="store_true", help="only the batched and serving measurements")
     ap.add_argument("--slots", type=int, default=8, help="serving slots (requests in flight)")
     ap.add_argument("--serve-requests", type=int, default=300)
@@ -254,6 +257,185 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def pick_energies(optical):
+    """Indices of three energies of a workload's grid for the precision samples: the low edge
+    of the range, the largest resonance (the largest summed delta and beta over the materials),
+    and the least contrast (the smallest spread of n^2 between the materials)."""
+    import numpy as np
+
+    o = np.asarray(optical, np.float64)
+    peak = int(np.argmax(o.sum(axis=(1, 2))))
+    n2p = (1.0 - o[..., 0] + 1j * o[..., 1]) ** 2
+    n2s = (1.0 - o[..., 2] + 1j * o[..., 3]) ** 2
+    spread = (np.abs(n2p - n2p.mean(axis=1, keepdims=True)).sum(axis=1)
+              + np.abs(n2s - n2s.mean(axis=1, keepdims=True)).sum(axis=1))
+    least = int(np.argmin(spread))
+    return {"low_edge": 0, "peak": peak, "least_contrast": least}
+
+
+def precision_study(args, w, energies, optical, host_vox, strategy):
+    """Full-size parity against the FP64 CPU oracle (the reference's per-angle algorithm):
+    the benchmark morphology at three energies (low edge, largest resonance, least contrast)
+    x 2 E angles; the first configuration in full (3 energies x 12 angles, both strategies);
+    the 128 x 512 x 512 configuration and the 256 x 1024 x 1024 precision study at their
+    largest resonance x 2 E angles.  Per entry: max relative error over pixels above 1e-6 of
+    the oracle's peak, and whether the NaN masks are identical.  The first headline sample's
+    oracle time is the CPU baseline."""
+    import numpy as np
+    import torch
+
+    from cyrsoxs_gb300 import _native, workloads
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+
+    oracle.build()
+    entries, cpu = [], None
+
+    def check(name, wl, es, opt, vox, angles, strat, per_energy_names=None):
+        o = _native.Options(nx=wl.nx, ny=wl.ny, nz=wl.nz, num_material=wl.num_material, energies=es,
+                            start_angle=angles[0], end_angle=angles[1], increment_angle=angles[2],
+                            phys_size=wl.phys_size, strategy=strat)
+        gpu = _native.cuda_main(o, opt, vox).astype(np.float64)
+        ref, secs = oracle.run_arrays(nx=wl.nx, ny=wl.ny, nz=wl.nz, energies=es, optical=opt, voxels=vox,
+                                      angles=angles, phys_size=wl.phys_size)
+        nang = int(round((angles[1] - angles[0]) / angles[2] + 1))
+        for i, e in enumerate(es):
+            err, npx = rel_err(gpu[i], ref[i])
+            entries.append({"config": name, "energy_eV": round(float(e), 4),
+                            "energy_kind": per_energy_names[i] if per_energy_names else None,
+                            "angles": nang, "strategy": {1: "per_energy", 2: "fields"}[strat],
+                            "max_rel_err": err, "pixels": npx,
+                            "nan_mask_equal": bool(np.array_equal(np.isnan(gpu[i]), np.isnan(ref[i])))})
+        return secs
+
+    two = lambda wl: (wl.angles[0], wl.angles[0] + wl.angles[2], wl.angles[2])  # noqa: E731
+    # benchmark morphology: three energies x 2 angles; the first energy alone times the CPU baseline
+    picks = pick_energies(optical)
+    idx = sorted(set(picks.values()))
+    kinds = {v: k for k, v in picks.items()}
+    secs = check(w.name, w, [energies[0]], optical[:1], host_vox, two(w), strategy, ["low_edge"])
+    cpu = {"value": 2.0 / secs, "unit": "patterns/s", "cores": oracle.num_threads(), "kind": "port",
+           "seconds": secs, "sample": "1 energy x 2 E angles of the same morphology (per-angle algorithm, FP64)"}
+    rest = [i for i in idx if i != 0]
+    if rest:
+        check(w.name, w, [energies[i] for i in rest], optical[rest], host_vox, two(w), strategy,
+              [kinds[i] for i in rest])
+    # first configuration in full, both strategies
+    c1 = workloads.workload("c1")
+    v1, o1 = workloads.voxels(c1), workloads.optical_constants(c1)
+    for strat in (1, 2):
+        check("c1", c1, c1.energies, o1, v1, c1.angles, strat)
+    del v1
+    # 128 x 512 x 512 (and 256 x 1024 x 1024): the largest resonance, 2 angles
+    for name in (("c2",) if args.skip_c4 else ("c2", "c4")):
+        wl = workloads.workload(name)
+        ol = workloads.optical_constants(wl)
+        p = pick_energies(ol)["peak"]
+        vl = workloads.voxels(wl)
+        torch.cuda.empty_cache()
+        check(name, wl, [wl.energies[p]], ol[p:p + 1], vl, two(wl), 2, ["peak"])
+        del vl
+        torch.cuda.empty_cache()
+    worst = max(e["max_rel_err"] for e in entries)
+    prec = {"max_rel_err_vs_fp64": worst, "nan_mask_equal": all(e["nan_mask_equal"] for e in entries),
+            "entries": entries, "threshold": "pixels above 1e-6 of the oracle's peak",
+            "oracle": "FP64 CPU restatement of the reference's per-angle algorithm"}
+    return prec, cpu
+
+
+def reference_gpu_baseline(args):
+    """The reference's own GPU path, unmodified (src/cudaMain.cu with cuFFT, NPP and cuBLAS,
+    built by oracle/ref/Makefile from the staged reference sources), timed on this GPU beside
+    the engine on the same requests.
+
+    Both sides are timed the same way: the wall clock around one full call from pinned host
+    buffers (cudaMain / cudaMainStreams in the reference's harness, cyr_cuda_main here), after
+    one untimed call; median of 2 timed calls.  The first configuration runs in full, with the
+    FP32 build (as shipped, --use_fast_math) for Algorithm 0 and 1 and the FP64 build for
+    Algorithm 0; the larger shapes run a 2-energy sample of their request (all E angles).
+    The engine's output is also compared with the reference FP64 build's where that ran."""
+    import tempfile
+
+    import numpy as np
+    import torch
+
+    from cyrsoxs_gb300 import _native, workloads
+    sys.path.insert(0, os.path.join(HERE, "tests", "golden"))
+    import cases
+
+    refdir = os.path.join(HERE, "oracle", "_ref")
+    if not os.path.exists(os.path.join(refdir, "cyrsoxs_ref_fp32")):
+        return {"unavailable": "the reference build (oracle/_ref) is missing: its sources were not staged"}
+    specs = [("c1", None, 0, "fp32"), ("c1", None, 1, "fp32"), ("c1", None, 0, "fp64"),
+             ("c2", 2, 0, "fp32"), ("c2", 2, 1, "fp32"), ("headline", 2, 0, "fp32")]
+    out, cache = [], {}
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True).numpy()
+        t[...] = a
+        return t
+
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, nsample, algo, prec in specs:
+            w = workloads.workload(name)
+            es = w.energies if nsample is None else w.energies[:nsample]
+            if name not in cache:
+                cache.clear()
+                torch.cuda.empty_cache()
+                cache[name] = (pinned(workloads.voxels(w)), workloads.optical_constants(w)[:len(es)])
+            vox, opt = cache[name]
+            case = cases.Case(name, w.nx, w.ny, w.nz, w.num_material, list(es), angles=tuple(w.angles),
+                              phys_size=w.phys_size, algorithm=algo, max_streams=1)
+            entry = {"config": f"{name}: Z x Y x X = {w.nz} x {w.ny} x {w.nx}, {w.num_material} materials, "
+                               f"{len(es)} energies x {w.num_angles()} E angles"
+                               + (" (sample of the request)" if nsample else ""),
+                     "algorithm": algo, "reference_build": prec, "patterns": len(es) * w.num_angles()}
+            if not cases.reference_reads_in_bounds(case):
+                entry["skipped"] = "the reference's Ewald gather would read outside the volume"
+                out.append(entry)
+                continue
+            cpath = os.path.join(tmp, "c.case")
+            rpath = os.path.join(tmp, "r.bin")
+            cases.write_case_arrays(case, cpath, opt, vox)
+            try:
+                p = subprocess.run([os.path.join(refdir, f"cyrsoxs_ref_{prec}"), cpath, rpath, "2"],
+                                   capture_output=True, text=True, timeout=900)
+            except subprocess.TimeoutExpired:
+                entry["error"] = "reference run timed out"
+                out.append(entry)
+                continue
+            if p.returncode != 0:
+                entry["error"] = f"reference exit code {p.returncode}: {(p.stdout + p.stderr)[-300:]}"
+                out.append(entry)
+                continue
+            rsec = [float(ln.split()[1]) for ln in p.stdout.splitlines() if ln.startswith("seconds ")]
+            o = _native.Options(nx=w.nx, ny=w.ny, nz=w.nz, num_material=w.num_material, energies=list(es),
+                                start_angle=w.angles[0], end_angle=w.angles[1], increment_angle=w.angles[2],
+                                phys_size=w.phys_size, algorithm=algo)
+            hout = torch.empty((len(es), 1, w.ny, w.nx), dtype=torch.float32, pin_memory=True).numpy()
+            _native.cuda_main(o, opt, vox, out=hout)  # untimed
+            esec = []
+            for _ in range(2):
+                t = time.perf_counter()
+                _native.cuda_main(o, opt, vox, out=hout)
+                esec.append(time.perf_counter() - t)
+            ref_s, eng_s = statistics.median(rsec), statistics.median(esec)
+            entry.update({"reference_s": ref_s, "reference_s_each": rsec, "engine_s": eng_s, "engine_s_each": esec,
+                          "reference_patterns_per_s": entry["patterns"] / ref_s,
+                          "engine_patterns_per_s": entry["patterns"] / eng_s, "engine_over_reference": ref_s / eng_s})
+            if prec == "fp64":
+                ref = np.fromfile(rpath, np.float64).reshape(hout.shape)
+                err, npx = rel_err(hout.astype(np.float64), ref)
+                entry["engine_vs_reference_fp64"] = {"max_rel_err": err, "pixels": npx, "nan_mask_equal": bool(
+                    np.array_equal(np.isnan(hout), np.isnan(ref)))}
+            out.append(entry)
+            print("reference_gpu", json.dumps(entry), file=sys.stderr, flush=True)
+    cache.clear()
+    return {"timing": "wall clock around one call from pinned host buffers, median of 2 after 1 untimed",
+            "builds": "reference sources unmodified; FP32 with --use_fast_math as shipped, FP64 -DDOUBLE_PRECISION",
+            "entries": out}
 
 
 def _pct(xs, q):
@@ -578,28 +760,15 @@ def main():
                      "api": "cyr_cuda_main (host buffers)"}
 
     if rank == 0 and world == 1 and not args.skip_cpu:
-        sys.path.insert(0, os.path.join(HERE, "oracle"))
-        import oracle
-
-        oracle.build()
-        two = (w.angles[0], w.angles[0] + w.angles[2], w.angles[2])
-        o2 = _native.Options(nx=w.nx, ny=w.ny, nz=w.nz, num_material=w.num_material, energies=energies[:1],
-                             start_angle=two[0], end_angle=two[1], increment_angle=two[2], phys_size=w.phys_size,
-                             strategy=2 if info["fields"] else 1)  # the strategy that was timed
-        gpu2 = _native.cuda_main(o2, optical[:1], host_vox_np).astype(np.float64)
-        ref2, secs = oracle.run_arrays(nx=w.nx, ny=w.ny, nz=w.nz, energies=energies[:1], optical=optical[:1],
-                                       voxels=host_vox_np, angles=two, phys_size=w.phys_size)
-        err, npx = rel_err(gpu2, ref2)
-        result["cpu_baseline"] = {"value": 2.0 / secs, "unit": "patterns/s", "cores": oracle.num_threads(),
-                                  "kind": "port", "seconds": secs,
-                                  "sample": "1 energy x 2 E angles of the same morphology (per-angle algorithm, FP64)"}
-        result["precision"] = {"max_rel_err_vs_fp64": err, "pixels": npx,
-                               "nan_mask_equal": bool(np.array_equal(np.isnan(gpu2), np.isnan(ref2))),
-                               "sample": "1 energy x 2 E angles, full-size morphology, pixels above 1e-6 of peak"}
+        result["precision"], result["cpu_baseline"] = precision_study(args, w, energies, optical, host_vox_np,
+                                                                      2 if info["fields"] else 1)
     if rank == 0 and world == 1 and not args.skip_served:
         del host_vox, host_vox_np
         torch.cuda.empty_cache()
         result["served"] = served_benchmarks(args)
+    if rank == 0 and world == 1 and not args.skip_reference_gpu:
+        torch.cuda.empty_cache()
+        result["reference_gpu"] = reference_gpu_baseline(args)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if dist is not None:

@@ -94,6 +94,16 @@ def run_arrays(*, nx, ny, nz, energies, optical, voxels, angles, phys_size, morp
     return out[:ne_out], float(secs[0])
 
 
+def polarization_case_file(path: str, shape):
+    """computePolarization debug path on a case file -> complex [3][nz][ny][nx]."""
+    nv = int(np.prod(shape[1:]))
+    out = np.zeros((3, nv, 2), np.float64)
+    rc = lib().oracle_polarization_case(path.encode(), _dp(out))
+    if rc:
+        raise RuntimeError(lib().oracle_last_error().decode())
+    return (out[..., 0] + 1j * out[..., 1]).reshape(shape)
+
+
 def polarization_case(case):
     import cases as _cases
 

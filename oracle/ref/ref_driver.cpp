@@ -25,12 +25,22 @@
 //   f32 voxels[num_material][nz][ny][nx][4]    (the reference's Voxel::s1)
 // Output: mode 0 -> f32/f64 projection [E][K][ny][nx];
 //         mode 1 -> px, py, pz complex [nz][ny][nx] each, in Real precision.
+//
+// Timing (baseline measurement): `<case.bin> <out.bin> <repeats>` runs the
+// mode-0 launch once untimed (CUDA context, cuFFT and NPP initialisation), then
+// <repeats> more times, printing "seconds <t>" for each: the wall clock
+// (std::chrono::steady_clock) around the whole cudaMain / cudaMainStreams call,
+// which returns once the projections are in host memory.  The voxel and
+// projection buffers are then pinned (cudaMallocHost), as the reference's
+// command line allocates them (src/main.cpp:136, include/cudaHeaders.h:85).
 
 #include <cudaMain.h>
 #include <RotationMatrix.h>
 
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <stdexcept>
@@ -62,10 +72,11 @@ struct Reader {
 }  // namespace
 
 int main(int argc, char **argv) {
-  if (argc != 3) {
-    std::fprintf(stderr, "usage: %s <case.bin> <out.bin>\n", argv[0]);
+  if (argc != 3 && argc != 4) {
+    std::fprintf(stderr, "usage: %s <case.bin> <out.bin> [timed repeats]\n", argv[0]);
     return 2;
   }
+  const int repeats = argc == 4 ? std::atoi(argv[3]) : 0;
   Reader r(argv[1]);
   char magic[8];
   r.in.read(magic, 8);
@@ -121,8 +132,16 @@ int main(int argc, char **argv) {
       mats[e * nmat + m].nperp.x = 1 - dper;
       mats[e * nmat + m].nperp.y = bper;
     }
-  std::vector<Voxel> voxels(size_t(nmat) * nvox);
-  for (size_t i = 0; i < voxels.size(); ++i) {
+  const size_t nvoxel_all = size_t(nmat) * nvox;
+  Voxel *voxels = nullptr;
+  std::vector<Voxel> voxels_pageable;
+  if (repeats > 0) {
+    if (cudaMallocHost(reinterpret_cast<void **>(&voxels), sizeof(Voxel) * nvoxel_all) != cudaSuccess) return 6;
+  } else {
+    voxels_pageable.resize(nvoxel_all);
+    voxels = voxels_pageable.data();
+  }
+  for (size_t i = 0; i < nvoxel_all; ++i) {
     voxels[i].s1.x = vox[4 * i + 0];
     voxels[i].s1.y = vox[4 * i + 1];
     voxels[i].s1.z = vox[4 * i + 2];
@@ -133,20 +152,34 @@ int main(int argc, char **argv) {
   std::ofstream out(argv[2], std::ios::binary);
   if (mode == 0) {
     const size_t total = size_t(ne) * in.kVectors.size() * size_t(nx) * ny;
-    std::vector<Real> proj(total, Real(0));
-    int rc;
-    if (in.algorithmType == Algorithm::CommunicationMinimizing)
-      rc = cudaMain(in.voxelDims, in, mats, proj.data(), rm, voxels.data());
-    else
-      rc = cudaMainStreams(in.voxelDims, in, mats, proj.data(), rm, voxels.data());
-    if (rc != EXIT_SUCCESS) return 4;
-    out.write(reinterpret_cast<const char *>(proj.data()), total * sizeof(Real));
+    std::vector<Real> proj_pageable;
+    Real *proj = nullptr;
+    if (repeats > 0) {
+      if (cudaMallocHost(reinterpret_cast<void **>(&proj), sizeof(Real) * total) != cudaSuccess) return 6;
+    } else {
+      proj_pageable.assign(total, Real(0));
+      proj = proj_pageable.data();
+    }
+    for (int call = 0; call <= repeats; ++call) {
+      std::memset(proj, 0, sizeof(Real) * total);
+      const auto t0 = std::chrono::steady_clock::now();
+      int rc;
+      if (in.algorithmType == Algorithm::CommunicationMinimizing)
+        rc = cudaMain(in.voxelDims, in, mats, proj, rm, voxels);
+      else
+        rc = cudaMainStreams(in.voxelDims, in, mats, proj, rm, voxels);
+      const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      if (rc != EXIT_SUCCESS) return 4;
+      if (call > 0) std::printf("seconds %.6f\n", secs);
+    }
+    std::fflush(stdout);
+    out.write(reinterpret_cast<const char *>(proj), total * sizeof(Real));
   } else {
     const auto &es = in.energies;
     const UINT eid = std::lower_bound(es.begin(), es.end(), Real(pol_energy)) - es.begin();
     std::vector<Complex> px(nvox), py(nvox), pz(nvox);
     const int rc = computePolarization(in.voxelDims, in, mats, px.data(), py.data(), pz.data(), rm,
-                                       voxels.data(), Real(pol_eangle), eid, static_cast<int>(nmat));
+                                       voxels, Real(pol_eangle), eid, static_cast<int>(nmat));
     if (rc != EXIT_SUCCESS) return 4;
     out.write(reinterpret_cast<const char *>(px.data()), nvox * sizeof(Complex));
     out.write(reinterpret_cast<const char *>(py.data()), nvox * sizeof(Complex));

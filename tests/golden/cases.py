@@ -134,8 +134,15 @@ def header_floats(case: Case):
 
 
 def write_case(case: Case, path: str) -> None:
-    opt = optical_constants(case)
-    vox = voxels(case)
+    write_case_arrays(case, path, optical_constants(case), voxels(case))
+
+
+def write_case_arrays(case: Case, path: str, opt: np.ndarray, vox: np.ndarray) -> None:
+    """The case file of `case` with the given optical constants [E][M][4] and voxels [M][Z][Y][X][4]."""
+    opt = np.ascontiguousarray(opt, np.float32)
+    vox = np.ascontiguousarray(vox, np.float32)
+    assert opt.shape == (len(case.energies), case.num_material, 4)
+    assert vox.shape == (case.num_material, case.nz, case.ny, case.nx, 4)
     with open(path, "wb") as f:
         f.write(b"CYRCASE1")
         f.write(struct.pack("<6I", case.nx, case.ny, case.nz, case.num_material, len(case.energies), len(case.kvecs)))
@@ -146,7 +153,7 @@ def write_case(case: Case, path: str) -> None:
         f.write(np.asarray(case.energies, np.float32).tobytes())
         f.write(np.asarray(case.kvecs, np.float32).reshape(-1).tobytes())
         f.write(opt.tobytes())
-        f.write(vox.tobytes())
+        vox.tofile(f)
 
 
 def num_angles(case: Case) -> int:
