@@ -93,6 +93,11 @@ def lib():
     L.cyr_stage_name.restype = ctypes.c_char_p
     L.cyr_num_stages.restype = ctypes.c_uint32
     L.cyr_release_scratch.argtypes = []
+    d_p = ctypes.POINTER(ctypes.c_double)
+    L.cyr_cuda_main_fp64.argtypes = [opt_p, d_p, d_p, d_p]
+    L.cyr_simulate_device_fp64.argtypes = [opt_p, d_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                           ctypes.c_void_p]
+    L.cyr_compute_polarization_fp64.argtypes = [opt_p, d_p, d_p, ctypes.c_double, ctypes.c_uint32, d_p, d_p, d_p]
     _lib = L
     return L
 
@@ -272,6 +277,54 @@ def profile_end():
         if launches[i]:
             out[lib().cyr_stage_name(i).decode()] = (int(launches[i]), float(ms[i]), int(calls[i]))
     return out, int(dropped.value)
+
+
+def _dptr(a: np.ndarray):
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 numpy array")
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def cuda_main_fp64(opts: Options, optical, voxels, out: np.ndarray | None = None) -> np.ndarray:
+    """The FP64 pipeline from host arrays (optical [E][M][4], voxels [M][Z][Y][X][4], both converted to
+    float64) -> float64 [E][K][ny][nx] (cyr_cuda_main_fp64)."""
+    s = opts.struct
+    shape = (s.num_energies, opts.num_k, s.ny, s.nx)
+    opt = np.ascontiguousarray(optical, np.float64)
+    vox = np.ascontiguousarray(voxels, np.float64)
+    if opt.size != s.num_energies * s.num_material * 4:
+        raise ValueError(f"optical has {opt.size} elements; these options need {s.num_energies * s.num_material * 4}")
+    if vox.size != voxel_count(opts):
+        raise ValueError(f"voxels has {vox.size} elements; these options need {voxel_count(opts)}")
+    if out is None:
+        out = np.empty(shape, np.float64)
+    if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != pattern_count(opts):
+        raise ValueError("out must be a C-contiguous float64 array of [E][K][Ny][Nx]")
+    check(lib().cyr_cuda_main_fp64(opts.ref, _dptr(opt), _dptr(vox), _dptr(out)))
+    return out
+
+
+def simulate_device_fp64(opts: Options, optical, d_voxels: int, voxels_fp64: bool, d_out: int, stream: int = 0) -> None:
+    """Device-resident FP64 pipeline: d_voxels float4 (voxels_fp64 False) or double4; d_out doubles."""
+    opt = np.ascontiguousarray(optical, np.float64)
+    if opt.size != opts.struct.num_energies * opts.struct.num_material * 4:
+        raise ValueError("optical constants do not match the options")
+    check(lib().cyr_simulate_device_fp64(opts.ref, _dptr(opt), ctypes.c_void_p(d_voxels), int(bool(voxels_fp64)),
+                                         ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
+
+
+def compute_polarization_fp64(opts: Options, optical, voxels, eangle: float, energy_id: int):
+    s = opts.struct
+    shape = (s.nz, s.ny, s.nx)
+    px, py, pz = (np.empty(shape, np.complex128) for _ in range(3))
+    opt = np.ascontiguousarray(optical, np.float64)
+    vox = np.ascontiguousarray(voxels, np.float64)
+    if vox.size != voxel_count(opts) or opt.size != s.num_energies * s.num_material * 4:
+        raise ValueError("arrays do not match the options")
+    as_d = lambda a: a.view(np.float64)  # noqa: E731
+    check(lib().cyr_compute_polarization_fp64(opts.ref, _dptr(opt), _dptr(vox), float(eangle), int(energy_id),
+                                              _dptr(as_d(px)), _dptr(as_d(py)), _dptr(as_d(pz))))
+    return px, py, pz
 
 
 def release_scratch() -> None:

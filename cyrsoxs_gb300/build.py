@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libcyrsoxs_gb300.so")
 SOURCES = ["engine.cu"]
-DEPS = SOURCES + ["kernels.cuh", "fields.cuh", "geometry.h"]
+DEPS = SOURCES + ["kernels.cuh", "fields.cuh", "fp64.cuh", "geometry.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -103,9 +103,9 @@ int run(const UINT *voxel, const InputData &in, const std::vector<Material> &mat
   make_request(voxel, in, mat, r);
   const Real *vox = &voxels[0].s1.x;
 #ifdef DOUBLE_PRECISION
+  if (streams) r.opt.algorithm = 1;  // Algorithm 1: no windowing, as cyr_cuda_main_streams
   const int rc = cyr_cuda_main_fp64(&r.opt, r.optical.data(), vox, projection);
-  (void)streams;  // the FP64 path runs Algorithm 0's schedule; Algorithm 1 differs only in windowing
-  return status(rc, "cudaMain (FP64)");
+  return status(rc, streams ? "cudaMainStreams (FP64)" : "cudaMain (FP64)");
 #else
   const int rc = streams ? cyr_cuda_main_streams(&r.opt, r.optical.data(), vox, projection)
                          : cyr_cuda_main(&r.opt, r.optical.data(), vox, projection);

@@ -54,6 +54,7 @@
 #include "geometry.h"
 #include "kernels.cuh"
 #include "fields.cuh"
+#include "fp64.cuh"
 
 namespace cyr {
 namespace {
@@ -111,6 +112,38 @@ uint32_t fft_lines_per_block(uint32_t n) {
   return tx;
 }
 
+bool smooth7(uint32_t n) {
+  std::vector<uint32_t> r;
+  return factorize(n, r);
+}
+
+// Lengths with a prime factor above 7 run as Bluestein transforms over the
+// smallest 7-smooth M >= 2N - 1, itself limited to one block's FFT.
+constexpr uint32_t kMaxBluesteinPad = 4096;
+uint32_t bluestein_length(uint32_t n) {
+  uint32_t m = 2 * n - 1;
+  while (!smooth7(m)) ++m;
+  return m;
+}
+
+// An axis length the FFT handles: 7-smooth within one block's shared memory,
+// or any other length whose Bluestein length is at most kMaxBluesteinPad.
+bool fft_length_ok(uint32_t n, const char **why) {
+  if (n <= 1) return true;
+  if (smooth7(n)) {
+    if (size_t(2) * n * 2 * sizeof(float2) > kFftSmemBudget) {
+      *why = "exceeds the single-block FFT limit";
+      return false;
+    }
+    return true;
+  }
+  if (n > (kMaxBluesteinPad + 1) / 2 || bluestein_length(n) > kMaxBluesteinPad) {
+    *why = "has a prime factor above 7 and exceeds the Bluestein limit of 2048";
+    return false;
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // Per-device context: cached twiddle tables and grow-only scratch.
 // ---------------------------------------------------------------------------
@@ -155,13 +188,13 @@ struct DeviceBuffer {
 // read back after the caller has synchronised (cyr_profile_end).
 enum Stage {
   kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kBuildZ,
-  kFieldMeans, kBuildFields, kEwaldFields, kRotateGram, kFftRows, kFftColsY, kFftColsZ, kNumStages
+  kFieldMeans, kBuildFields, kEwaldFields, kRotateGram, kFftRows, kFftColsY, kFftColsZ, kBluestein, kNumStages
 };
 const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_pass<y>", "k_fft_pass<z>", "k_dc",
                                              "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp",
                                              "k_moments", "k_entry_means", "k_build_fft_z",
                                              "k_field_means", "k_build_fields", "k_ewald_fields", "k_rotate_gram",
-                                             "k_fft_rows", "k_fft_cols<y>", "k_fft_cols<z>"};
+                                             "k_fft_rows", "k_fft_cols<y>", "k_fft_cols<z>", "k_bluestein"};
 
 struct Profiler {
   bool active = false;
@@ -197,6 +230,7 @@ struct ZTune {
 // share the device context's; every serving slot owns one.
 struct Scratch {
   DeviceBuffer spec, images, avg, params, dc, moments, means, errors, conv, flags, fmean;
+  DeviceBuffer blue;               // padded lines of the Bluestein transforms
   cudaEvent_t last_use = nullptr;  // completion of the last request that used it
   uint64_t generation = 0;         // bumped by every (re)allocation of a buffer above
   int init() {
@@ -205,16 +239,16 @@ struct Scratch {
   }
   // serving slots: stream-ordered allocations on `st`
   void bind(cudaStream_t st) {
-    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean})
+    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue})
       b->stream = st, b->generation = &generation;
   }
   void release() {
-    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean})
+    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue})
       b->release();
   }
   size_t bytes() const {
     size_t n = 0;
-    for (const DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean})
+    for (const DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue})
       n += b->bytes;
     return n;
   }
@@ -228,6 +262,15 @@ struct DeviceContext {
   std::map<std::string, ZTune> ztune;  // key: nx,ny,nz,nmat,nvol,morphology
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
+  struct BlueTables {
+    uint32_t m = 0;
+    float2 *chirp = nullptr, *bhat = nullptr;
+  };
+  std::map<uint32_t, BlueTables> blue;  // per Bluestein line length
+  std::map<uint32_t, double2 *> tw64;   // FP64 twiddles W_n^m per length
+  struct Fp64Scratch {
+    DeviceBuffer spec, images, avg, params, params64, vox, out;
+  } f64;                                // the FP64 pipeline's buffers (plain entry points)
   Scratch main;
   DeviceBuffer vox_in, out_in;  // host-buffer entry points: morphology and projections
   // TMA column passes: the driver's tensor-map encoder, and a word set when a
@@ -490,17 +533,120 @@ int thread_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
   return CYR_OK;
 }
 
+// Chirp c_j = exp(-i pi j^2 / n) and bhat = FFT_m(b) / m, b_j = conj(c_j) at j
+// and m - j: in double (j^2 mod 2n in integers, a direct DFT with exact index
+// arithmetic), rounded to float, once per length and device.
+int get_blue(DeviceContext &ctx, uint32_t n, DeviceContext::BlueTables &out) {
+  std::lock_guard<std::mutex> lk(ctx.tables_mu);
+  auto it = ctx.blue.find(n);
+  if (it != ctx.blue.end()) {
+    out = it->second;
+    return CYR_OK;
+  }
+  const uint32_t m = bluestein_length(n);
+  std::vector<std::complex<double>> c(n), b(m, 0.0), w(m);
+  for (uint32_t j = 0; j < n; ++j) {
+    const uint64_t q = (uint64_t(j) * j) % (2 * uint64_t(n));
+    c[j] = std::polar(1.0, -kPi * double(q) / double(n));
+  }
+  for (uint32_t j = 0; j < n; ++j) {
+    b[j] = std::conj(c[j]);
+    if (j) b[m - j] = std::conj(c[j]);
+  }
+  for (uint32_t j = 0; j < m; ++j) w[j] = std::polar(1.0, -2.0 * kPi * double(j) / double(m));
+  std::vector<float2> hc(n), hb(m);
+  for (uint32_t j = 0; j < n; ++j) hc[j] = make_float2(float(c[j].real()), float(c[j].imag()));
+  for (uint32_t k = 0; k < m; ++k) {
+    std::complex<double> acc(0.0, 0.0);
+    uint64_t idx = 0;  // (j k) mod m
+    for (uint32_t j = 0; j < m; ++j, idx += k) {
+      if (idx >= m) idx %= m;
+      acc += b[j] * w[idx];
+    }
+    acc /= double(m);
+    hb[k] = make_float2(float(acc.real()), float(acc.imag()));
+  }
+  DeviceContext::BlueTables t;
+  t.m = m;
+  CYR_CUDA(cudaMalloc(&t.chirp, sizeof(float2) * n));
+  CYR_CUDA(cudaMalloc(&t.bhat, sizeof(float2) * m));
+  CYR_CUDA(cudaMemcpy(t.chirp, hc.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+  CYR_CUDA(cudaMemcpy(t.bhat, hb.data(), sizeof(float2) * m, cudaMemcpyHostToDevice));
+  ctx.blue[n] = t;
+  out = t;
+  return CYR_OK;
+}
+
+int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
+             int first, int last, size_t vstride = 0, DeviceBuffer *work = nullptr);
+
+// One axis of length n (a prime factor above 7) as a Bluestein transform, in
+// chunks of padded lines of at most 256 MB held in `work`.
+int bluestein_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
+                   cudaStream_t st, size_t vstride, DeviceBuffer *work) {
+  const uint32_t n = axis == 0 ? nx : axis == 1 ? ny : nz;
+  DeviceContext::BlueTables bt;
+  CYR_TRY(get_blue(ctx, n, bt));
+  const uint32_t lpv = axis == 0 ? ny * nz : axis == 1 ? nx * nz : nx * ny;
+  const uint64_t total = uint64_t(lpv) * count;
+  const uint64_t cap = std::max<uint64_t>(1, (size_t(256) << 20) / (size_t(bt.m) * sizeof(float2)));
+  const uint32_t chunk = uint32_t(std::min<uint64_t>(total, cap));
+  CYR_TRY(work->ensure(size_t(chunk) * bt.m * sizeof(float2)));
+  int sms = 0;
+  CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  BlueParams p{};
+  p.data = data;
+  p.work = work->as<float2>();
+  p.chirp = bt.chirp;
+  p.bhat = bt.bhat;
+  p.nx = nx, p.ny = ny, p.nz = nz;
+  p.vstride = vstride;
+  p.n = n, p.m = bt.m;
+  p.lines_per_vol = lpv;
+  for (uint64_t l0 = 0; l0 < total; l0 += chunk) {
+    p.line0 = l0;
+    p.nlines = uint32_t(std::min<uint64_t>(chunk, total - l0));
+    const size_t elems = size_t(p.nlines) * bt.m;
+    const unsigned grid = unsigned(std::min<size_t>((elems + 255) / 256, size_t(sms) * 16));
+    int slot = ctx.prof.begin(kBluestein, st);
+    if (axis == 0) k_blue_gather<0><<<grid, 256, 0, st>>>(p);
+    if (axis == 1) k_blue_gather<1><<<grid, 256, 0, st>>>(p);
+    if (axis == 2) k_blue_gather<2><<<grid, 256, 0, st>>>(p);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+    CYR_TRY(fft_axes(ctx, p.work, bt.m, p.nlines, 1, 1, st, 0, 0));  // m is 7-smooth
+    slot = ctx.prof.begin(kBluestein, st);
+    k_blue_mul<<<grid, 256, 0, st>>>(p);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+    CYR_TRY(fft_axes(ctx, p.work, bt.m, p.nlines, 1, 1, st, 0, 0));
+    slot = ctx.prof.begin(kBluestein, st);
+    if (axis == 0) k_blue_scatter<0><<<grid, 256, 0, st>>>(p);
+    if (axis == 1) k_blue_scatter<1><<<grid, 256, 0, st>>>(p);
+    if (axis == 2) k_blue_scatter<2><<<grid, 256, 0, st>>>(p);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+  }
+  return CYR_OK;
+}
+
 // In-place forward FFT of `count` volumes along the axes [first, last]
 // (0 x, 1 y, 2 z).  vstride (elements between volumes) defaults to the volume
 // size; a larger one runs the x and y passes on nz planes of larger volumes
 // (data pointing at the first plane), as the slab pipeline does.
+// Lengths with a prime factor above 7 use `work` (default: the device's main
+// scratch, for callers holding the context lock).
 int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
-             int first, int last, size_t vstride = 0) {
+             int first, int last, size_t vstride, DeviceBuffer *work) {
   const size_t nvox = vstride ? vstride : size_t(nx) * ny * nz;
   const uint32_t dims[3] = {nx, ny, nz};
   for (int axis = first; axis <= last; ++axis) {
     const uint32_t n = dims[axis];
     if (n == 1) continue;
+    if (!smooth7(n)) {
+      CYR_TRY(bluestein_pass(ctx, data, nx, ny, nz, count, axis, st, nvox, work ? work : &ctx.main.blue));
+      continue;
+    }
     if (n == 128 || n == 256 || n == 512 || n == 1024) {
       CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st, nvox));
       continue;
@@ -536,8 +682,8 @@ int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_
 }
 
 int fft3d(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
-          bool skip_z = false) {
-  return fft_axes(ctx, data, nx, ny, nz, count, st, 0, skip_z ? 1 : 2);
+          bool skip_z = false, DeviceBuffer *work = nullptr) {
+  return fft_axes(ctx, data, nx, ny, nz, count, st, 0, skip_z ? 1 : 2, 0, work);
 }
 
 // ---------------------------------------------------------------------------
@@ -741,14 +887,11 @@ int validate(const cyr_options *o) {
   if (size_t(o->nx) * o->ny * o->nz > kMaxVolumeVoxels)
     return fail(CYR_ERR_UNSUPPORTED, "volume of %u x %u x %u voxels exceeds the limit of 2^32 - 1 voxels", o->nx, o->ny,
                 o->nz);
-  std::vector<uint32_t> r;
   const uint32_t d[3] = {o->nx, o->ny, o->nz};
-  for (uint32_t n : d)
-    if (n > 1 && !factorize(n, r))
-      return fail(CYR_ERR_UNSUPPORTED, "dimension %u has a prime factor above 7 (supported: 2^a 3^b 5^c 7^d)", n);
-  for (uint32_t n : d)
-    if (n > 1 && size_t(2) * n * 2 * sizeof(float2) > kFftSmemBudget)
-      return fail(CYR_ERR_UNSUPPORTED, "dimension %u exceeds the single-block FFT limit", n);
+  for (uint32_t n : d) {
+    const char *why = "";
+    if (!fft_length_ok(n, &why)) return fail(CYR_ERR_UNSUPPORTED, "dimension %u %s", n, why);
+  }
   return CYR_OK;
 }
 
@@ -822,7 +965,7 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
     pl.zwarp = true;
     kept_planes(o, pl);
     pl.vstride = size_t(pl.kz) * pl.npix;
-  } else if (!pl.twod) {
+  } else if (!pl.twod && smooth7(pl.nz)) {
     // fused build + z FFT: lines per block so that two 512-thread blocks fit an SM
     uint32_t tx = 16;
     while (tx > 1 && (size_t(2) * pl.nvol * pl.nz * (tx + 1) + pl.nz) * sizeof(float2) > 104 * 1024) tx /= 2;
@@ -1133,10 +1276,10 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
       k_build_fields<1><<<blocks, 256, 0, st>>>(fp);
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
-    CYR_TRY(fft_axes(ctx, spec + fp.i0, pl.nx, pl.ny, z1 - z0, npk, st, 0, 1, pl.nvox));
+    CYR_TRY(fft_axes(ctx, spec + fp.i0, pl.nx, pl.ny, z1 - z0, npk, st, 0, 1, pl.nvox, &sc.blue));
     if (up) CYR_TRY(const_cast<SlabUpload *>(up)->issue(sl + 1));  // the next slab's copy, behind this slab's kernels
   }
-  CYR_TRY(fft_axes(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st, 2, 2));
+  CYR_TRY(fft_axes(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st, 2, 2, 0, &sc.blue));
   // bin 0 of each packed volume replaced by the mean of its neighbours
   CYR_TRY(sc.dc.ensure(size_t(kMaxPacked) * sizeof(float2)));
   int slot = ctx.prof.begin(kDc, st);
@@ -1495,7 +1638,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
         ctx.prof.end(slot, st);
       }
       CYR_CUDA(cudaGetLastError());
-      CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.kz, bp.nvol, st, true));
+      CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.kz, bp.nvol, st, true, &sc.blue));
     } else {
       slot = ctx.prof.begin(kBuild, st, o->morphology_type == 0 ? 2 : 1);
       if (o->morphology_type == 0) {
@@ -1506,7 +1649,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
       }
       ctx.prof.end(slot, st);
       CYR_CUDA(cudaGetLastError());
-      CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, bp.nvol, st));
+      CYR_TRY(fft3d(ctx, spec, pl.nx, pl.ny, pl.nz, bp.nvol, st, false, &sc.blue));
     }
     slot = ctx.prof.begin(kDc, st);
     k_dc<<<1, 32, 0, st>>>(spec, bp.nvol, pl.vstride, pl.nx, pl.ny, pl.nz, pl.p0, pl.p1, pl.pn, dc);
@@ -1615,6 +1758,233 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
   return CYR_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// FP64 pipeline (fp64.cuh): geometry from the FP32 planner (float decisions),
+// amplitudes in double.
+// ---------------------------------------------------------------------------
+int get_tw64(DeviceContext &ctx, uint32_t n, const double2 **tw) {
+  std::lock_guard<std::mutex> lk(ctx.tables_mu);
+  auto it = ctx.tw64.find(n);
+  if (it != ctx.tw64.end()) {
+    *tw = it->second;
+    return CYR_OK;
+  }
+  std::vector<double2> h(n);
+  for (uint32_t m = 0; m < n; ++m) {
+    const std::complex<double> w = std::polar(1.0, -2.0 * kPi * double(m) / double(n));
+    h[m] = make_double2(w.real(), w.imag());
+  }
+  double2 *d = nullptr;
+  CYR_CUDA(cudaMalloc(&d, sizeof(double2) * n));
+  CYR_CUDA(cudaMemcpy(d, h.data(), sizeof(double2) * n, cudaMemcpyHostToDevice));
+  ctx.tw64[n] = d;
+  *tw = d;
+  return CYR_OK;
+}
+
+constexpr size_t kFft64Smem = 192 * 1024;
+
+// In-place forward FFT of `count` double volumes (7-smooth lengths).
+int fft64(DeviceContext &ctx, double2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st) {
+  static std::once_flag attrs;
+  cudaError_t ea = cudaSuccess;
+  std::call_once(attrs, [&] {
+    ea = cudaFuncSetAttribute(k64_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem));
+    if (ea == cudaSuccess) ea = cudaFuncSetAttribute(k64_fft<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem));
+    if (ea == cudaSuccess) ea = cudaFuncSetAttribute(k64_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem));
+  });
+  CYR_CUDA(ea);
+  const uint32_t dims[3] = {nx, ny, nz};
+  const size_t vstride = size_t(nx) * ny * nz;
+  for (int axis = 0; axis < 3; ++axis) {
+    const uint32_t n = dims[axis];
+    if (n == 1) continue;
+    std::vector<uint32_t> r;
+    if (!factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FP64 path: length %u has a prime factor above 7", n);
+    Fft64Params p{};
+    p.data = data;
+    p.nx = nx, p.ny = ny, p.nz = nz;
+    p.vstride = vstride;
+    p.n = n;
+    p.nstages = uint32_t(r.size());
+    for (size_t i = 0; i < r.size(); ++i) p.radix_code |= uint64_t(r[i]) << (4 * i);
+    CYR_TRY(get_tw64(ctx, n, &p.tw));
+    uint32_t tx = 16;
+    while (tx > 1 && size_t(2) * n * tx * sizeof(double2) > 96 * 1024) tx /= 2;
+    p.tx = tx;
+    const size_t smem = size_t(2) * n * tx * sizeof(double2);
+    if (smem > kFft64Smem) return fail(CYR_ERR_UNSUPPORTED, "FP64 path: length %u too large for one block", n);
+    const uint32_t tiles = axis == 0 ? (ny * nz + tx - 1) / tx : ((nx + tx - 1) / tx) * (axis == 1 ? nz : ny);
+    const dim3 grid(tiles, count);
+    if (axis == 0) k64_fft<0><<<grid, 256, smem, st>>>(p);
+    if (axis == 1) k64_fft<1><<<grid, 256, smem, st>>>(p);
+    if (axis == 2) k64_fft<2><<<grid, 256, smem, st>>>(p);
+    CYR_CUDA(cudaGetLastError());
+  }
+  return CYR_OK;
+}
+
+// The FP64 path's double tables, uploaded beside the planner's float arena:
+// refractive indices per energy, Hanning tables and the E basis coefficients.
+struct Plan64 {
+  std::vector<unsigned char> arena;
+  size_t off_mat = 0, off_hx = 0, off_hy = 0, off_hz = 0, off_e = 0;
+};
+
+int make_plan64(const cyr_options *o, const double *optical, bool window, Plan &pl, Plan64 &p64) {
+  CYR_TRY(validate(o));
+  if (!optical) return fail(CYR_ERR_ARGUMENT, "optical constants pointer is null");
+  for (uint32_t n : {o->nx, o->ny, o->nz})
+    if (n > 1 && !smooth7(n))
+      return fail(CYR_ERR_UNSUPPORTED, "FP64 path: dimension %u has a prime factor above 7 (7-smooth lengths only)", n);
+  // geometry (k frames, E rotations, q tables, warp coefficients) from the FP32 planner
+  std::vector<float> of(size_t(o->num_energies) * o->num_material * 4);
+  for (size_t i = 0; i < of.size(); ++i) of[i] = float(optical[i]);
+  CYR_TRY(make_plan(o, of.data(), pl));
+  std::vector<Mat64> mats(pl.ne);
+  for (uint32_t e = 0; e < pl.ne; ++e) {
+    std::memset(&mats[e], 0, sizeof(Mat64));
+    for (uint32_t m = 0; m < pl.nmat; ++m) {
+      const double *op = optical + (size_t(e) * pl.nmat + m) * 4;
+      mats[e].npar[m] = make_double2(1.0 - op[0], op[1]);
+      mats[e].nper[m] = make_double2(1.0 - op[2], op[3]);
+    }
+  }
+  p64.arena.clear();
+  p64.off_mat = arena_put(p64.arena, mats.data(), mats.size());
+  auto hann = [&](uint32_t n, bool unit) {
+    std::vector<double> w(n);
+    for (uint32_t j = 0; j < n; ++j) w[j] = unit || !window ? 1.0 : 0.5 * (1 - std::cos(2 * kPi * j / n));
+    return w;
+  };
+  const std::vector<double> hx = hann(pl.nx, false), hy = hann(pl.ny, false), hz = hann(pl.nz, pl.twod);
+  p64.off_hx = arena_put(p64.arena, hx.data(), hx.size());
+  p64.off_hy = arena_put(p64.arena, hy.data(), hy.size());
+  p64.off_hz = arena_put(p64.arena, hz.data(), hz.size());
+  std::vector<double> ecoef(size_t(pl.nk) * pl.nang * pl.nbasis);
+  for (size_t ka = 0; ka < size_t(pl.nk) * pl.nang; ++ka)
+    for (uint32_t b = 0; b < pl.nbasis; ++b)
+      ecoef[ka * pl.nbasis + b] = pl.material_frame ? 1.0 : double(pl.evec[ka * 3 + b]);
+  p64.off_e = arena_put(p64.arena, ecoef.data(), ecoef.size());
+  p64.arena.resize((p64.arena.size() + 255) & ~size_t(255));
+  return CYR_OK;
+}
+
+int run_fp64(DeviceContext &ctx, const cyr_options *o, const double *optical, const void *d_vox, bool vox64,
+             double *d_out, cudaStream_t st) {
+  Plan pl;
+  Plan64 p64;
+  CYR_TRY(make_plan64(o, optical, o->algorithm == 0 && o->windowing == 1, pl, p64));
+  auto &f = ctx.f64;
+  const uint32_t nvol = pl.material_frame ? 3u : pl.nvol;
+  CYR_TRY(f.spec.ensure(size_t(nvol) * pl.nvox * sizeof(double2)));
+  CYR_TRY(f.images.ensure(size_t(pl.nang) * pl.npix * sizeof(double)));
+  CYR_TRY(f.avg.ensure(pl.npix * sizeof(double)));
+  CYR_TRY(f.params.ensure(pl.arena.size()));
+  CYR_TRY(f.params64.ensure(p64.arena.size()));
+  CYR_CUDA(cudaMemcpyAsync(f.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st));
+  CYR_CUDA(cudaMemcpyAsync(f.params64.ptr, p64.arena.data(), p64.arena.size(), cudaMemcpyHostToDevice, st));
+  const unsigned char *dp = f.params.as<unsigned char>(), *dq = f.params64.as<unsigned char>();
+  double2 *spec = f.spec.as<double2>();
+  double *images = f.images.as<double>(), *avg = f.avg.as<double>();
+  int sms = 0;
+  CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  Build64Params bp{};
+  bp.vox = d_vox;
+  bp.vox_fp64 = vox64 ? 1u : 0u;
+  bp.nx = pl.nx, bp.ny = pl.ny, bp.nz = pl.nz, bp.nmat = pl.nmat;
+  bp.nvox = pl.nvox;
+  bp.morphology = o->morphology_type;
+  bp.material_frame = pl.material_frame ? 1u : 0u;
+  if (pl.hanning) {
+    bp.hann_x = reinterpret_cast<const double *>(dq + p64.off_hx);
+    bp.hann_y = reinterpret_cast<const double *>(dq + p64.off_hy);
+    bp.hann_z = reinterpret_cast<const double *>(dq + p64.off_hz);
+  }
+  const unsigned bgrid = unsigned(std::min<size_t>((pl.nvox + 255) / 256, size_t(sms) * 8));
+  const unsigned pgrid = unsigned((pl.npix + 255) / 256);
+  const int W = int(pl.ny), H = int(pl.nx);  // the reference hands NPP width = Ny, height = Nx
+  const WarpCoef *dwarp = reinterpret_cast<const WarpCoef *>(dp + pl.off_warp);
+  const double *dE = reinterpret_cast<const double *>(dq + p64.off_e);
+  const Mat64 *dmat = reinterpret_cast<const Mat64 *>(dq + p64.off_mat);
+  const double prefill = o->rot_mask ? 0.0 : std::numeric_limits<double>::quiet_NaN();
+  for (uint32_t e = 0; e < pl.ne; ++e) {
+    const float wavelength = static_cast<float>(1239.84197 / o->energies[e]);  // src/cudaMain.cu:607-608
+    const float kmag = static_cast<float>(2 * kPi / wavelength);
+    auto spectra = [&](uint32_t nv) -> int {
+      bp.nvol = nv;
+      bp.out = spec;
+      k64_build<<<bgrid, 256, 0, st>>>(bp, dmat + e);
+      CYR_CUDA(cudaGetLastError());
+      CYR_TRY(fft64(ctx, spec, pl.nx, pl.ny, pl.nz, nv, st));
+      k64_dc<<<1, 32, 0, st>>>(spec, nv, pl.nvox, pl.nx, pl.ny, pl.nz);
+      CYR_CUDA(cudaGetLastError());
+      return CYR_OK;
+    };
+    if (!pl.material_frame) {
+      bp.mode = 0;
+      CYR_TRY(spectra(nvol));
+    }
+    for (uint32_t k = 0; k < pl.nk; ++k) {
+      const KFrame &fr = pl.frames[k];
+      Ewald64Params ep{};
+      ep.spec = spec;
+      ep.vstride = pl.nvox;
+      ep.g.start = -static_cast<float>(kPi / o->phys_size);
+      ep.g.dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nx - 1) * 1.0));
+      ep.g.dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.ny - 1) * 1.0));
+      ep.g.dz = pl.twod ? 0.f : static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nz - 1) * 1.0));
+      ep.g.kmag = kmag;
+      ep.g.kx = kmag * fr.k.x, ep.g.ky = kmag * fr.k.y, ep.g.kz = kmag * fr.k.z;
+      ep.g.nx = pl.nx, ep.g.ny = pl.ny, ep.g.nz = pl.nz;
+      ep.g.interp = o->ewald_interpolation;
+      ep.g.twod = pl.twod ? 1u : 0u;
+      ep.qx = reinterpret_cast<const float *>(dp + pl.off_qx);
+      ep.qy = reinterpret_cast<const float *>(dp + pl.off_qy);
+      ep.qz = reinterpret_cast<const float *>(dp + pl.off_qz);
+      if (!pl.material_frame) {
+        const uint32_t sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+        ep.nbasis = pl.nbasis;
+        for (int c = 0; c < 3; ++c)
+          for (uint32_t b = 0; b < pl.nbasis; ++b) ep.vol[c][b] = sym[c][b];
+        ep.nangles = pl.nang;
+        ep.E = dE + size_t(k) * pl.nang * pl.nbasis;
+        ep.images = images;
+        k64_ewald<<<pgrid, 256, 0, st>>>(ep);
+        CYR_CUDA(cudaGetLastError());
+      } else {
+        // per angle, as the reference: p = R^T Nt R x -> 3 transforms -> Ewald into image a
+        for (uint32_t a = 0; a < pl.nang; ++a) {
+          const size_t ka = size_t(k) * pl.nang + a;
+          bp.mode = 1;
+          for (int c = 0; c < 3; ++c) bp.E[c] = double(pl.evec[ka * 3 + c]);
+          for (int i = 0; i < 9; ++i) bp.R[i] = double(pl.rmats[ka].m[i]);
+          CYR_TRY(spectra(3));
+          ep.nbasis = 1;
+          for (int c = 0; c < 3; ++c) ep.vol[c][0] = uint32_t(c);
+          ep.nangles = 1;
+          ep.E = dE + ka;  // coefficient 1
+          ep.images = images + size_t(a) * pl.npix;
+          k64_ewald<<<pgrid, 256, 0, st>>>(ep);
+          CYR_CUDA(cudaGetLastError());
+        }
+      }
+      Rotate64Params rp{};
+      rp.images = images;
+      rp.coef = dwarp + size_t(k) * pl.nang;
+      rp.W = W, rp.H = H;
+      rp.nangles = pl.nang;
+      rp.rot_mask = o->rot_mask;
+      rp.avg = avg;
+      k64_rotate_average<<<pgrid, 256, 0, st>>>(rp);
+      k64_warp<<<pgrid, 256, 0, st>>>(avg, d_out + (size_t(e) * pl.nk + k) * pl.npix, W, H, pl.detector_warp[k],
+                                      prefill);
+      CYR_CUDA(cudaGetLastError());
+    }
+  }
+  return CYR_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Serving engine: continuous batching of simulation requests on one GPU.
@@ -1999,6 +2369,9 @@ int cyr_release_scratch(void) {
   ctx->main.release();
   ctx->vox_in.release();
   ctx->out_in.release();
+  for (DeviceBuffer *b : {&ctx->f64.spec, &ctx->f64.images, &ctx->f64.avg, &ctx->f64.params, &ctx->f64.params64,
+                          &ctx->f64.vox, &ctx->f64.out})
+    b->release();
   return CYR_OK;
 }
 
@@ -2134,6 +2507,109 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
   return rc;
 }
 
+int cyr_cuda_main_fp64(const cyr_options *opt, const double *optical, const double *voxels, double *projection) {
+  if (!voxels || !projection) return fail(CYR_ERR_ARGUMENT, "host pointer is null");
+  CYR_TRY(validate(opt));
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  const size_t nvox = size_t(opt->nx) * opt->ny * opt->nz;
+  const size_t vox_bytes = nvox * opt->num_material * 4 * sizeof(double);
+  const uint32_t nk = (opt->case_type == 0 && (opt->num_k == 0 || !opt->k_vectors)) ? 1u : opt->num_k;
+  const size_t out_bytes = size_t(opt->num_energies) * nk * opt->nx * opt->ny * sizeof(double);
+  CYR_TRY(ctx->f64.vox.ensure(vox_bytes));
+  CYR_TRY(ctx->f64.out.ensure(out_bytes));
+  cudaStream_t st = nullptr;
+  CYR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  int rc = CYR_OK;
+  do {
+    if (cudaMemcpyAsync(ctx->f64.vox.ptr, voxels, vox_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "voxel upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    if ((rc = run_fp64(*ctx, opt, optical, ctx->f64.vox.ptr, true, ctx->f64.out.as<double>(), st)) != CYR_OK) break;
+    if (cudaMemcpyAsync(projection, ctx->f64.out.ptr, out_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "projection download failed: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(CYR_ERR_CUDA, "FP64 simulation failed: %s", cudaGetErrorString(e));
+  } while (false);
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  return rc;
+}
+
+int cyr_simulate_device_fp64(const cyr_options *opt, const double *optical, const void *d_voxels,
+                             uint32_t voxels_fp64, double *d_projection, void *stream) {
+  if (!d_voxels || !d_projection) return fail(CYR_ERR_ARGUMENT, "device pointer is null");
+  if (voxels_fp64 > 1) return fail(CYR_ERR_ARGUMENT, "voxels_fp64 must be 0 (float4) or 1 (double4)");
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return run_fp64(*ctx, opt, optical, d_voxels, voxels_fp64 == 1, d_projection, static_cast<cudaStream_t>(stream));
+}
+
+int cyr_compute_polarization_fp64(const cyr_options *opt, const double *optical, const double *voxels, double eangle,
+                                  uint32_t energy_id, double *px, double *py, double *pz) {
+  if (!voxels || !px || !py || !pz) return fail(CYR_ERR_ARGUMENT, "host pointer is null");
+  if (opt && opt->case_type != 0) return fail(CYR_ERR_UNSUPPORTED, "only implemented for case type 0 (as the reference)");
+  Plan pl;
+  Plan64 p64;
+  // the debug path windows whatever the algorithm (src/cudaMain.cu:1722-1725)
+  CYR_TRY(make_plan64(opt, optical, opt->windowing == 1, pl, p64));
+  if (energy_id >= pl.ne) return fail(CYR_ERR_ARGUMENT, "energy id out of range");
+  DeviceContext *ctx = nullptr;
+  CYR_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto &f = ctx->f64;
+  const size_t vox_bytes = pl.nvox * pl.nmat * 4 * sizeof(double);
+  CYR_TRY(f.vox.ensure(vox_bytes));
+  CYR_TRY(f.spec.ensure(3 * pl.nvox * sizeof(double2)));
+  CYR_TRY(f.params64.ensure(p64.arena.size()));
+  cudaStream_t st = nullptr;
+  CYR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  int rc = CYR_OK;
+  do {
+    cudaMemcpyAsync(f.params64.ptr, p64.arena.data(), p64.arena.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(f.vox.ptr, voxels, vox_bytes, cudaMemcpyHostToDevice, st);
+    const unsigned char *dq = f.params64.as<unsigned char>();
+    Build64Params bp{};
+    bp.vox = f.vox.ptr;
+    bp.vox_fp64 = 1;
+    bp.nx = pl.nx, bp.ny = pl.ny, bp.nz = pl.nz, bp.nmat = pl.nmat;
+    bp.nvox = pl.nvox;
+    bp.morphology = opt->morphology_type;
+    bp.mode = 1;
+    bp.nvol = 3;
+    bp.material_frame = pl.material_frame ? 1u : 0u;
+    // the debug path rotates E by EAngle radians about k (src/cudaMain.cu:1716-1721)
+    const Mat3f R = e_rotation(pl.frames[0], float(eangle));
+    for (int c = 0; c < 3; ++c) bp.E[c] = double(R.m[c * 3 + 0]);
+    for (int i = 0; i < 9; ++i) bp.R[i] = double(R.m[i]);
+    if (opt->windowing == 1) {
+      bp.hann_x = reinterpret_cast<const double *>(dq + p64.off_hx);
+      bp.hann_y = reinterpret_cast<const double *>(dq + p64.off_hy);
+      bp.hann_z = reinterpret_cast<const double *>(dq + p64.off_hz);
+    }
+    bp.out = f.spec.as<double2>();
+    const unsigned blocks = unsigned(std::min<size_t>((pl.nvox + 255) / 256, 65535));
+    k64_build<<<blocks, 256, 0, st>>>(bp, reinterpret_cast<const Mat64 *>(dq + p64.off_mat) + energy_id);
+    if (cudaGetLastError() != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "polarization kernel launch failed");
+      break;
+    }
+    const size_t cb = pl.nvox * sizeof(double2);
+    cudaMemcpyAsync(px, f.spec.as<double2>(), cb, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(py, f.spec.as<double2>() + pl.nvox, cb, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(pz, f.spec.as<double2>() + 2 * pl.nvox, cb, cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(CYR_ERR_CUDA, "FP64 polarization failed: %s", cudaGetErrorString(e));
+  } while (false);
+  cudaStreamDestroy(st);
+  return rc;
+}
+
 int cyr_profile_begin(uint32_t max_launches) {
   DeviceContext *ctx = nullptr;
   CYR_TRY(get_context(&ctx));
@@ -2188,9 +2664,10 @@ int cyr_fft3d_device(void *d_data, uint32_t nx, uint32_t ny, uint32_t nz, uint32
   if (!d_data || nx < 1 || ny < 1 || nz < 1 || count < 1) return fail(CYR_ERR_ARGUMENT, "bad FFT arguments");
   if (size_t(nx) * ny * nz > kMaxVolumeVoxels)
     return fail(CYR_ERR_ARGUMENT, "volume of %u x %u x %u elements exceeds the limit of 2^32 - 1", nx, ny, nz);
-  std::vector<uint32_t> r;
-  for (uint32_t n : {nx, ny, nz})
-    if (n > 1 && !factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u has a prime factor above 7", n);
+  for (uint32_t n : {nx, ny, nz}) {
+    const char *why = "";
+    if (!fft_length_ok(n, &why)) return fail(CYR_ERR_UNSUPPORTED, "FFT length %u %s", n, why);
+  }
   if (count > 65535) return fail(CYR_ERR_ARGUMENT, "too many volumes in one call");
   DeviceContext *ctx = nullptr;
   CYR_TRY(get_context(&ctx));

@@ -545,6 +545,101 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
 }
 
 // ---------------------------------------------------------------------------
+// Bluestein (chirp-z) transform, for line lengths N with a prime factor above 7
+// (cuFFT's cufftPlan3d accepts every size, src/cudaMain.cu:479-482).
+//
+// With c_j = exp(-i pi j^2 / N), jk = (j^2 + k^2 - (k - j)^2) / 2 gives
+//   X_k = c_k sum_j (x_j c_j) conj(c_{k-j}),
+// a circular convolution of length M >= 2N - 1 (M 7-smooth), evaluated as
+// FFT_M -> product with the table bhat = FFT_M(b) / M, where b holds
+// conj(c_m) at m and M - m -> a second FFT_M of the conjugate, since the
+// inverse transform is conj(FFT(conj(y))) / M.  Chirp and table are formed in
+// double on the host (j^2 reduced mod 2N in integers) and rounded to float.
+// The lines of a pass are processed in chunks of `nlines` padded lines held
+// in `work` [nlines][M]; consecutive threads take consecutive x for y and z
+// lines, so the strided gathers and scatters stay coalesced.
+// ---------------------------------------------------------------------------
+struct BlueParams {
+  float2 *data;           // the volumes being transformed
+  float2 *work;           // [nlines][m]
+  const float2 *chirp;    // c_j, j < n
+  const float2 *bhat;     // FFT_m(b) / m
+  uint32_t nx, ny, nz;    // volume dimensions (nz: the planes this call covers)
+  size_t vstride;         // elements between volumes
+  uint32_t n, m;          // line length, padded length
+  uint64_t line0;         // first line of this chunk
+  uint32_t nlines;        // lines in this chunk
+  uint32_t lines_per_vol; // x pass: ny nz; y pass: nx nz; z pass: nx ny
+};
+
+// Offset of line `line` and the stride between its elements.
+template <int AXIS>
+__device__ __forceinline__ size_t blue_line(const BlueParams &p, uint64_t line, size_t &estep) {
+  const uint64_t v = line / p.lines_per_vol;
+  const uint32_t r = uint32_t(line % p.lines_per_vol);
+  size_t base = v * p.vstride;
+  if (AXIS == 0) {
+    base += size_t(r) * p.nx;
+    estep = 1;
+  } else if (AXIS == 1) {
+    base += size_t(r / p.nx) * p.nx * p.ny + r % p.nx;
+    estep = p.nx;
+  } else {
+    base += size_t(r / p.nx) * p.nx + r % p.nx;
+    estep = size_t(p.nx) * p.ny;
+  }
+  return base;
+}
+
+// work[l][j] = x_j c_j (j < n), 0 (n <= j < m)
+template <int AXIS>
+__global__ void k_blue_gather(BlueParams p) {
+  const size_t total = size_t(p.nlines) * p.m;
+  for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
+    uint32_t l, j;
+    if (AXIS == 0) {
+      l = uint32_t(t / p.m), j = uint32_t(t % p.m);
+    } else {
+      l = uint32_t(t % p.nlines), j = uint32_t(t / p.nlines);
+    }
+    float2 v = make_float2(0.f, 0.f);
+    if (j < p.n) {
+      size_t es;
+      const size_t b = blue_line<AXIS>(p, p.line0 + l, es);
+      v = cmul(p.data[b + j * es], p.chirp[j]);
+    }
+    p.work[size_t(l) * p.m + j] = v;
+  }
+}
+
+// work = conj(work * bhat): the product of the transforms, conjugated for the inverse
+__global__ void k_blue_mul(BlueParams p) {
+  const size_t total = size_t(p.nlines) * p.m;
+  for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
+    const float2 w = cmul(p.work[t], p.bhat[t % p.m]);
+    p.work[t] = make_float2(w.x, -w.y);
+  }
+}
+
+// x_k = c_k conj(work[l][k]), k < n
+template <int AXIS>
+__global__ void k_blue_scatter(BlueParams p) {
+  const size_t total = size_t(p.nlines) * p.n;
+  for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
+    uint32_t l, k;
+    if (AXIS == 0) {
+      l = uint32_t(t / p.n), k = uint32_t(t % p.n);
+    } else {
+      l = uint32_t(t % p.nlines), k = uint32_t(t / p.nlines);
+    }
+    const float2 w = p.work[size_t(l) * p.m + k];
+    size_t es;
+    const size_t b = blue_line<AXIS>(p, p.line0 + l, es);
+    p.data[b + k * es] = cmul(p.chirp[k], make_float2(w.x, -w.y));
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Warp-level FFT for power-of-two lengths N = 32 V (V = 4, 8, 16, 32).
 //
 // One warp owns one line.  Lane t holds x[t + 32 i] in v[i] (natural order)

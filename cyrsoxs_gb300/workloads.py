@@ -5,7 +5,11 @@ benchmark configurations (no public dataset is involved).
   is a sphere of radius 40 voxels (vfrac 1 inside) in a matrix of material 1;
   S = 0.5; theta, psi uniform random per voxel; 280/285/290 eV with
   delta = beta = 1e-3 + 5e-3 L(E) (Lorentzian at 285 eV, 1 eV wide);
-  E angles 0:15:165.
+  E angles 0:15:165.  Both materials get the same isotropic constants, so
+  the dielectric tensor is (n^2 - 1) I everywhere and only the DC bin is
+  non-zero: the patterns are rounding noise.  ``c1_aniso`` is the same case
+  with the perpendicular resonance amplitude halved, which gives the
+  orientation field contrast; precision is checked on it.
 * ``c2`` / ``headline``: 4 materials; vfrac from seeded smooth random fields
   arg-maxed into 4 phases and smoothed over ~3 voxels; S ~ U(0, 1); a smooth
   random director field (theta = acos n_z, psi = atan2(n_y, n_x)); energies
@@ -57,6 +61,9 @@ def _lorentz(e, e0, width):
 def workload(name: str, energies=None) -> Workload:
     if name == "c1":
         return Workload("c1", 32, 256, 256, 2, energies or [280.0, 285.0, 290.0], (0.0, 165.0, 15.0), 5.0, 0, "sphere")
+    if name == "c1_aniso":
+        return Workload("c1_aniso", 32, 256, 256, 2, energies or [280.0, 285.0, 290.0], (0.0, 165.0, 15.0), 5.0, 0,
+                        "sphere", extra={"perp_amplitude": 0.5})
     if name == "c2":
         es = energies or [float(e) for e in np.linspace(270.0, 300.0, 50)]
         return Workload("c2", 128, 512, 512, 4, es, (0.0, 175.0, 5.0), 2.0, 2, "random")
@@ -107,10 +114,12 @@ def _smooth_sizes(lo: int, hi: int) -> list:
 def serving_stream(n_requests: int, rate: float = 200.0, seed: int = 5) -> list:
     """The serving configuration: Poisson arrivals (mean `rate` per second) of
     requests whose volume is log-uniform between 32 x 128^2 and 128 x 512^2
-    voxels, quantised to FFT-friendly sizes, with 2-4 materials, 1-100
-    energies and 6-36 E angles.  Returns [(arrival_s, Workload)].  (Sizes with
-    prime factors above 7 are rejected by the engine, so none are drawn.)"""
+    voxels, with 2-4 materials, 1-100 energies and 6-36 E angles.  95% of the
+    sizes are quantised to FFT-friendly lengths (2^a 3^b 5^c 7^d); 5% keep
+    arbitrary lengths (prime factors above 7 run as Bluestein transforms).
+    Returns [(arrival_s, Workload)]."""
     rng = np.random.Generator(np.random.PCG64(seed))
+    arbitrary = np.random.Generator(np.random.PCG64(seed + 1)).uniform(size=n_requests) < 0.05
     xy_sizes = _smooth_sizes(128, 512)
     z_sizes = _smooth_sizes(32, 128)
     t, out = 0.0, []
@@ -121,6 +130,9 @@ def serving_stream(n_requests: int, rate: float = 200.0, seed: int = 5) -> list:
         side = (4.0 * vol) ** (1.0 / 3.0)
         xy = min(xy_sizes, key=lambda n: abs(math.log(n / side)))
         z = min(z_sizes, key=lambda n: abs(math.log(n / max(32.0, min(128.0, vol / (xy * xy))))))
+        if arbitrary[i]:
+            xy = int(min(512, max(128, round(side))))
+            z = int(min(128, max(32, round(vol / (xy * xy)))))
         m = int(rng.integers(2, 5))
         ne = int(rng.integers(1, 101))
         na = int(rng.integers(6, 37))
@@ -134,9 +146,11 @@ def optical_constants(w: Workload) -> np.ndarray:
     """[E][M][4] float32."""
     out = np.zeros((len(w.energies), w.num_material, 4), np.float64)
     if w.kind == "sphere":
+        perp = w.extra.get("perp_amplitude", 1.0)
         for i, e in enumerate(w.energies):
-            v = 1e-3 + 5e-3 * _lorentz(e, 285.0, 1.0)
-            out[i, :, :] = v
+            L = _lorentz(e, 285.0, 1.0)
+            out[i, :, 0:2] = 1e-3 + 5e-3 * L
+            out[i, :, 2:4] = 1e-3 + perp * 5e-3 * L
         return out.astype(np.float32)
     rng = np.random.Generator(np.random.PCG64(w.seed + 17))
     for m in range(w.num_material):

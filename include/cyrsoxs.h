@@ -110,6 +110,36 @@ CYR_API int cyr_compute_polarization(const cyr_options *opt, const float *optica
                              uint32_t energy_id, float *px, float *py, float *pz);
 
 /*
+ * FP64 pipeline: the drop-in for the reference's -DDOUBLE_PRECISION build
+ * (include/Datatypes.h:33-46: Real = double, Voxel::s1 a double4, cuFFT Z2Z),
+ * with the same contract as cyr_cuda_main (include/cudaMain.h:53-60) on
+ * double arrays: optical [E][M][4], voxels [M][Z][Y][X][4], projection
+ * [E][K][Ny][Nx].  Every amplitude is computed in double (tensor, window, FFT,
+ * DC replacement, intensity, interpolation, warps, angle mean); the discrete
+ * decisions (NaN pixels, Ewald planes, warp taps) are made in float exactly as
+ * the FP32 path makes them, so the NaN masks equal cyr_cuda_main's.  Axis
+ * lengths must be 7-smooth (2^a 3^b 5^c 7^d).
+ */
+CYR_API int cyr_cuda_main_fp64(const cyr_options *opt, const double *optical, const double *voxels, double *projection);
+
+/*
+ * Device-resident FP64 pipeline: d_voxels holds float4 (voxels_fp64 = 0, the
+ * FP32 path's own input, so the two can be compared on one morphology) or
+ * double4 (voxels_fp64 = 1) voxels; d_projection receives doubles.
+ * Asynchronous on `stream`; scratch is kept by the library (per device).
+ */
+CYR_API int cyr_simulate_device_fp64(const cyr_options *opt, const double *optical, const void *d_voxels,
+                                     uint32_t voxels_fp64, double *d_projection, void *stream);
+
+/*
+ * FP64 polarization of one energy for an E rotation of eangle RADIANS:
+ * replaces the FP64 build's computePolarization (include/cudaMain.h:71-87,
+ * src/cudaMain.cu:1669-1738).  px/py/pz receive complex double [nz][ny][nx].
+ */
+CYR_API int cyr_compute_polarization_fp64(const cyr_options *opt, const double *optical, const double *voxels,
+                                          double eangle, uint32_t energy_id, double *px, double *py, double *pz);
+
+/*
  * Device-resident variant: voxels and projection are device pointers on the
  * current device; stream is a cudaStream_t (0 = legacy default stream).  The
  * call is asynchronous with respect to the host once it returns CYR_OK.

@@ -125,8 +125,8 @@ def test_invalid_options_are_rejected_before_any_device_work():
     with pytest.raises(nat.CyrError) as ei:
         nat.required_device_bytes(opts)
     assert ei.value.code == 1
-    bad = nat.Options(nx=22, ny=8, nz=4, num_material=1, energies=[285.0], start_angle=0, end_angle=0,
-                      increment_angle=0, phys_size=5.0)  # 22 = 2 * 11: prime factor above 7
+    bad = nat.Options(nx=4099, ny=8, nz=4, num_material=1, energies=[285.0], start_angle=0, end_angle=0,
+                      increment_angle=0, phys_size=5.0)  # prime, beyond the Bluestein limit
     with pytest.raises(nat.CyrError) as ei:
         nat.required_device_bytes(bad)
     assert ei.value.code == 2
@@ -154,7 +154,7 @@ GOOD = dict(nx=16, ny=16, nz=8, num_material=2, energies=[285.0], start_angle=0.
     (dict(start_angle=90.0, end_angle=0.0), 1, "start angle"),
     (dict(increment_angle=0.0), 1, "increment angle is 0"),
     (dict(end_angle=4096.0, increment_angle=0.5), 1, "angle count"),
-    (dict(nz=13), 2, "prime factor"),
+    (dict(nz=2053), 2, "Bluestein limit"),  # prime: its padded length would exceed one block's FFT
     (dict(nx=6561, ny=2, nz=1), 2, "single-block FFT limit"),  # 3^8: factorable, above one block
     (dict(nx=2048, ny=2048, nz=1024), 2, "2^32"),  # 2^32 voxels: beyond 32-bit offsets in a volume
 ], ids=lambda v: str(v) if not isinstance(v, dict) else ",".join(f"{k}={w}" for k, w in v.items()))
@@ -170,7 +170,9 @@ def test_edge_shapes_that_are_valid_plan_on_the_host():
     nat = _native()
     for over in (dict(nz=1), dict(nx=2, ny=2, nz=1), dict(num_material=32), dict(start_angle=30.0, end_angle=30.0,
                                                                                    increment_angle=0.0),
-                 dict(nx=7, ny=5, nz=3), dict(end_angle=4095.0, increment_angle=1.0)):
+                 dict(nx=7, ny=5, nz=3), dict(end_angle=4095.0, increment_angle=1.0),
+                 # lengths with a prime factor above 7 run as Bluestein transforms
+                 dict(nx=101, ny=97, nz=13), dict(nx=2039, ny=2, nz=1), dict(nx=22, ny=8, nz=4)):
         assert nat.required_device_bytes(nat.Options(**{**GOOD, **over})) > 0
 
 

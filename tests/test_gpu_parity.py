@@ -60,7 +60,10 @@ def rel_err(a, ref, thr=1e-6):
                                          ((16, 64, 40), 2), ((32, 8, 16), 1),
                                          # TMA column passes: 32-column tiles, 16-column tiles (nx not a
                                          # multiple of 32), 512-point lines on several volumes
-                                         ((4, 256, 64), 2), ((256, 4, 48), 1), ((2, 256, 80), 2), ((2, 512, 16), 3)])
+                                         ((4, 256, 64), 2), ((256, 4, 48), 1), ((2, 256, 80), 2), ((2, 512, 16), 3),
+                                         # Bluestein: lengths with a prime factor above 7 on every axis
+                                         ((3, 11, 13), 2), ((2, 97, 101), 1), ((61, 6, 40), 1), ((2, 4, 2039), 1),
+                                         ((17, 256, 48), 1), ((5, 127, 64), 2), ((1, 22, 1031), 1)])
 def test_fft3d_matches_numpy(shape, count):
     torch = _torch()
     nat = native()
@@ -193,4 +196,25 @@ def test_strategies_agree_and_auto_picks_fields_for_many_energies():
     assert nat.plan_info(options_for(case))["fields"] == 1
     assert np.array_equal(np.isnan(per), np.isnan(fld))
     e = rel_err(fld.astype(np.float64), per.astype(np.float64))
+    assert e.max() <= TOL, e.max()
+
+
+# Lengths with a prime factor above 7 (Bluestein transforms on the affected axes), both strategies.
+PRIME = [
+    cases.Case("prime_xyz", 37, 29, 11, 2, [282.0, 286.0], seed=51, geometry="blobs", angles=(0.0, 150.0, 30.0)),
+    cases.Case("prime_z_vector", 32, 32, 23, 3, [285.0], seed=52, morphology=cases.VECTOR, geometry="blobs",
+               angles=(0.0, 90.0, 45.0)),
+    cases.Case("prime_x_2d", 101, 64, 1, 2, [284.0], seed=53, geometry="blobs", angles=(0.0, 120.0, 60.0)),
+]
+
+
+@pytest.mark.parametrize("strategy", [1, 2])
+@pytest.mark.parametrize("case", PRIME, ids=[c.name for c in PRIME])
+def test_prime_lengths_match_oracle(case, strategy):
+    nat = native()
+    got = nat.cuda_main(options_for(case, strategy=strategy), cases.optical_constants(case),
+                        cases.voxels(case)).astype(np.float64)
+    want = oracle.run_case(case)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    e = rel_err(got, want)
     assert e.max() <= TOL, e.max()

@@ -48,10 +48,15 @@ MIX = ["euler_sphere", "vector_nn_full", "euler_hanning_mask", "material_frame",
        "odd_sizes", "alg1_streams", "four_materials", "nonsquare", "c1_slice"]
 
 
+# a size with prime factors above 7 on every axis (Bluestein transforms)
+EXTRA = {"prime_mix": cases.Case("prime_mix", 37, 29, 11, 2, [283.0, 287.0], seed=61, geometry="blobs",
+                                 angles=(0.0, 150.0, 30.0))}
+
+
 def mix_requests(nat):
     reqs = []
-    for i, n in enumerate(MIX):
-        c = cases.CASES[n]
+    for i, n in enumerate(MIX + list(EXTRA)):
+        c = EXTRA[n] if n in EXTRA else cases.CASES[n]
         strategy = (0, 1, 2)[i % 3]
         reqs.append((n, options_for(nat, c, strategy=strategy), cases.optical_constants(c),
                      np.ascontiguousarray(cases.voxels(c), np.float32), c))
