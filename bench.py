@@ -47,6 +47,7 @@ sys.path.insert(0, HERE)
 
 METRIC = "patterns/s (512²×256, ≤1e-4 rel vs FP64) batched vs plain; p50/p99 latency"
 ENERGIES_PER_STEP = 50  # one full request of the workload (50 energies x 36 E angles)
+REF_CALLS = 5  # timed calls per side in the reference GPU comparison
 
 
 def parse():
@@ -173,6 +174,7 @@ def algorithmic_bytes(kernel, w, nvol, nang, planes, batch=1, npk=0):
         nq = 4 * (6 if nvol == 6 else 3)  # Gram bytes per pixel and energy (packed records)
         table = {
             "k_build_fields": (16 * M + 8 * npk) * V,
+            "k_build_fields_rows": (16 * M + 8 * npk) * V,  # build fused with the x pass: one write
             "k_moments": 16 * M * P * math.ceil(w.nz / max(1, w.nz // 16)),  # every (nz / 16)-th z plane
             "k_fft_rows": 2 * 8 * npk * V,
             "k_fft_cols<y>": 2 * 8 * npk * V,
@@ -423,7 +425,8 @@ def reference_gpu_baseline(args):
 
     Both sides are timed the same way: the wall clock around one full call from pinned host
     buffers (cudaMain / cudaMainStreams in the reference's harness, cyr_cuda_main here), after
-    one untimed call; median of 2 timed calls.  The first configuration runs in full, with the
+    one untimed call; median of REF_CALLS timed calls (the shared host link shows occasional
+    100 ms stalls on either side).  The first configuration runs in full, with the
     FP32 build (as shipped, --use_fast_math) for Algorithm 0 and 1 and the FP64 build for
     Algorithm 0; the larger shapes run a 2-energy sample of their request (all E angles).
     The engine's output is also compared with the reference FP64 build's where that ran."""
@@ -471,7 +474,7 @@ def reference_gpu_baseline(args):
             rpath = os.path.join(tmp, "r.bin")
             cases.write_case_arrays(case, cpath, opt, vox)
             try:
-                p = subprocess.run([os.path.join(refdir, f"cyrsoxs_ref_{prec}"), cpath, rpath, "2"],
+                p = subprocess.run([os.path.join(refdir, f"cyrsoxs_ref_{prec}"), cpath, rpath, str(REF_CALLS)],
                                    capture_output=True, text=True, timeout=900)
             except subprocess.TimeoutExpired:
                 entry["error"] = "reference run timed out"
@@ -488,7 +491,7 @@ def reference_gpu_baseline(args):
             hout = torch.empty((len(es), 1, w.ny, w.nx), dtype=torch.float32, pin_memory=True).numpy()
             _native.cuda_main(o, opt, vox, out=hout)  # untimed
             esec = []
-            for _ in range(2):
+            for _ in range(REF_CALLS):
                 t = time.perf_counter()
                 _native.cuda_main(o, opt, vox, out=hout)
                 esec.append(time.perf_counter() - t)
@@ -508,7 +511,7 @@ def reference_gpu_baseline(args):
             out.append(entry)
             print("reference_gpu", json.dumps(entry), file=sys.stderr, flush=True)
     cache.clear()
-    return {"timing": "wall clock around one call from pinned host buffers, median of 2 after 1 untimed",
+    return {"timing": f"wall clock around one call from pinned host buffers, median of {REF_CALLS} after 1 untimed",
             "builds": "reference sources unmodified; FP32 with --use_fast_math as shipped, FP64 -DDOUBLE_PRECISION",
             "entries": out}
 

@@ -40,7 +40,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp"
+    # host float geometry (k frames, rotations, warp coefficients) without fused multiply-adds, so that it
+    # rounds as the reference's x86 build and the oracle do on every host architecture
     cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", *ARCH, "-shared", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-ffp-contract=off",
            "-Xcompiler", "-fvisibility=hidden", "-DCYR_BUILDING_LIBRARY", "-I", os.path.join(REPO, "include"),
            *[os.path.join(CSRC, s) for s in SOURCES], "-o", tmp, "-lcudart"]
     if verbose:

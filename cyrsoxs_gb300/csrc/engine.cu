@@ -41,6 +41,7 @@
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -188,13 +189,15 @@ struct DeviceBuffer {
 // read back after the caller has synchronised (cyr_profile_end).
 enum Stage {
   kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kBuildZ,
-  kFieldMeans, kBuildFields, kEwaldFields, kRotateGram, kFftRows, kFftColsY, kFftColsZ, kBluestein, kNumStages
+  kFieldMeans, kBuildFields, kEwaldFields, kRotateGram, kFftRows, kFftColsY, kFftColsZ, kBluestein, kBuildFieldsRows,
+  kNumStages
 };
 const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_pass<y>", "k_fft_pass<z>", "k_dc",
                                              "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp",
                                              "k_moments", "k_entry_means", "k_build_fft_z",
                                              "k_field_means", "k_build_fields", "k_ewald_fields", "k_rotate_gram",
-                                             "k_fft_rows", "k_fft_cols<y>", "k_fft_cols<z>", "k_bluestein"};
+                                             "k_fft_rows", "k_fft_cols<y>", "k_fft_cols<z>", "k_bluestein",
+                                             "k_build_fields_rows"};
 
 struct Profiler {
   bool active = false;
@@ -254,12 +257,29 @@ struct Scratch {
   }
 };
 
+// Launch forms of a y or z column pass (autotuned per shape on the FIELDS path):
+// TMA tiles with a producer warp (32-column tiles for 256-point lines when nx
+// allows, 16 for 512, 8 for 1024), the block-synchronous TMA form (256-point
+// lines), or cp.async tiles.  All forms run the same warp FFT, so their
+// results are identical; kFormAuto is the fixed choice below.
+enum ColForm : uint32_t { kFormAuto = 0, kFormTmaWs = 1, kFormTmaSync = 2, kFormCp = 3 };
+const char *form_name(uint32_t f) {
+  return f == kFormTmaWs ? "tma_ws" : f == kFormTmaSync ? "tma_sync" : f == kFormCp ? "cp_async" : "auto";
+}
+
 struct DeviceContext {
   int device = -1;
   Profiler prof;
   std::mutex mu;         // the plain entry points (they share `main`)
   std::mutex tables_mu;  // twiddles, autotuning results, kernel attributes
   std::map<std::string, ZTune> ztune;  // key: nx,ny,nz,nmat,nvol,morphology
+  struct FieldTune {
+    uint32_t form[3] = {kFormAuto, kFormAuto, kFormAuto};  // per axis (y and z tuned)
+    bool fused = true;                                     // field build fused with the x pass
+    std::string report;
+  };
+  std::map<std::string, FieldTune> ftune;  // key: nx,ny,nz,npk (FIELDS path)
+  bool autotune = true;                    // CYRSOXS_GB300_AUTOTUNE=0 keeps the fixed choices
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
   struct BlueTables {
@@ -295,6 +315,8 @@ int get_context(DeviceContext **out) {
   if (!slot) {
     slot.reset(new DeviceContext);
     slot->device = dev;
+    const char *env = std::getenv("CYRSOXS_GB300_AUTOTUNE");
+    slot->autotune = !(env && std::strcmp(env, "0") == 0);
   }
   *out = slot.get();
   return CYR_OK;
@@ -337,8 +359,17 @@ int setup_attrs(DeviceContext &ctx) {
                                 int(cols_tma_ws_smem<1>(512))));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(cols_tma_ws_smem<2>(256))));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(cols_tma_ws_smem<1>(128))));
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(cols_tma_ws_smem<2>(128))));
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma64<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(cols_tma64_smem(1024))));
+#define CYR_ROWS_ATTR(M, V) \
+  CYR_CUDA(cudaFuncSetAttribute(k_build_fields_rows<M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CYR_ROWS_ATTR(0, 4) CYR_ROWS_ATTR(0, 8) CYR_ROWS_ATTR(0, 16) CYR_ROWS_ATTR(0, 32)
+  CYR_ROWS_ATTR(1, 4) CYR_ROWS_ATTR(1, 8) CYR_ROWS_ATTR(1, 16) CYR_ROWS_ATTR(1, 32)
+#undef CYR_ROWS_ATTR
   {
     cudaDriverEntryPointQueryResult q{};
     void *fn = nullptr;
@@ -406,10 +437,10 @@ int encode_cols_map(DeviceContext &ctx, CUtensorMap *map, void *data, uint32_t n
   return CYR_OK;
 }
 
-// One axis of the 3D FFT with the warp-level kernels (n = 128, 256, 512).
+// One axis of the 3D FFT with the warp-level kernels (n = 128, 256, 512, 1024).
 template <int V>
 int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
-                    cudaStream_t st, size_t nvox) {
+                    cudaStream_t st, size_t nvox, uint32_t form = kFormAuto) {
   constexpr uint32_t N = 32 * V;
   const float2 *tw = nullptr;
   CYR_TRY(get_twiddles(ctx, N, &tw));
@@ -418,7 +449,7 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     RowPassParams rp{data, uint32_t(size_t(ny) * nz * count), tw, ny * nz, nvox};
     const size_t smem = (N + 8 * N) * sizeof(float2);
     k_fft_rows<V><<<(rp.rows + 7) / 8, 256, smem, st>>>(rp);
-  } else if (V == 32 && nx % 8 == 0 && ctx.encode_tiled && ctx.tma_error) {
+  } else if (V == 32 && nx % 8 == 0 && ctx.encode_tiled && ctx.tma_error && form != kFormCp) {
     // 1024-point lines: 8-column tiles (k_fft_cols_tma64)
     CUtensorMap map;
     CYR_TRY(encode_cols_map(ctx, &map, data, nx, ny, nz, count, nvox, axis, 256, 8));
@@ -434,7 +465,8 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma64<32>, 9 * 32, cols_tma64_smem(N)));
     const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
     k_fft_cols_tma64<32><<<grid, 9 * 32, cols_tma64_smem(N), st>>>(map, tp);
-  } else if ((V == 8 || V == 16) && nx % kTmaCols == 0 && ctx.encode_tiled && ctx.tma_error) {
+  } else if ((V == 4 || V == 8 || V == 16) && nx % kTmaCols == 0 && ctx.encode_tiled && ctx.tma_error &&
+             form != kFormCp) {
     CUtensorMap map;
     CYR_TRY(encode_cols_map(ctx, &map, data, nx, ny, nz, count, nvox, axis, N < 256 ? N : 256));
     ColTmaParams tp{};
@@ -446,11 +478,27 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     tp.error = ctx.tma_error;
     int sms = 0, per_sm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+    // 128-point lines: 32 (nx a multiple of 32) or 16 columns with a producer warp;
     // 256-point lines: tiles of 32 columns with a producer warp (nx a multiple of
     // 32; 256-byte runs per line), else the block-synchronous 16-column form;
     // 512-point lines: 16 columns with a producer warp
-    if constexpr (V == 8) {
-      if (nx % (2 * kTmaCols) == 0) {
+    if constexpr (V == 4) {
+      auto launch_ws = [&](auto hc) -> int {
+        constexpr int HH = decltype(hc)::value;
+        tp.nxt = nx / (HH * kTmaCols);
+        tp.ntiles = tp.nxt * tp.others * count;
+        CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<4, HH>, (8 * HH + 1) * 32,
+                                                               cols_tma_ws_smem<HH>(N)));
+        const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
+        k_fft_cols_tma_ws<4, HH><<<grid, (8 * HH + 1) * 32, cols_tma_ws_smem<HH>(N), st>>>(map, tp);
+        return CYR_OK;
+      };
+      if (nx % (2 * kTmaCols) == 0)
+        CYR_TRY(launch_ws(std::integral_constant<int, 2>{}));
+      else
+        CYR_TRY(launch_ws(std::integral_constant<int, 1>{}));
+    } else if constexpr (V == 8) {
+      if (nx % (2 * kTmaCols) == 0 && form != kFormTmaSync) {
         tp.nxt = nx / (2 * kTmaCols);
         tp.ntiles = tp.nxt * tp.others * count;
         CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<8, 2>, 17 * 32,
@@ -498,12 +546,26 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
 }
 
 int warp_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
-                  cudaStream_t st, size_t nvox) {
+                  cudaStream_t st, size_t nvox, uint32_t form = kFormAuto) {
   const uint32_t n = axis == 0 ? nx : axis == 1 ? ny : nz;
-  if (n == 128) return warp_fft_pass_v<4>(ctx, data, nx, ny, nz, count, axis, st, nvox);
-  if (n == 256) return warp_fft_pass_v<8>(ctx, data, nx, ny, nz, count, axis, st, nvox);
-  if (n == 512) return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st, nvox);
-  return warp_fft_pass_v<32>(ctx, data, nx, ny, nz, count, axis, st, nvox);
+  if (n == 128) return warp_fft_pass_v<4>(ctx, data, nx, ny, nz, count, axis, st, nvox, form);
+  if (n == 256) return warp_fft_pass_v<8>(ctx, data, nx, ny, nz, count, axis, st, nvox, form);
+  if (n == 512) return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st, nvox, form);
+  return warp_fft_pass_v<32>(ctx, data, nx, ny, nz, count, axis, st, nvox, form);
+}
+
+// The forms that apply to a column pass of n-point lines (axis 1 or 2) for this nx.
+std::vector<uint32_t> column_forms(const DeviceContext &ctx, uint32_t n, uint32_t nx) {
+  std::vector<uint32_t> f;
+  const bool tma = ctx.encode_tiled && ctx.tma_error;
+  if (n == 256 && tma && nx % kTmaCols == 0) {
+    if (nx % (2 * kTmaCols) == 0) f.push_back(kFormTmaWs);
+    f.push_back(kFormTmaSync);
+  }
+  if ((n == 128 || n == 512) && tma && nx % kTmaCols == 0) f.push_back(kFormTmaWs);
+  if (n == 1024 && tma && nx % 8 == 0) f.push_back(kFormTmaWs);
+  if (n == 128 || n == 256 || n == 512 || n == 1024) f.push_back(kFormCp);
+  return f;
 }
 
 // One y or z pass with k_fft_thread (lines of 8..64, one thread per line).
@@ -578,7 +640,7 @@ int get_blue(DeviceContext &ctx, uint32_t n, DeviceContext::BlueTables &out) {
 }
 
 int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
-             int first, int last, size_t vstride = 0, DeviceBuffer *work = nullptr);
+             int first, int last, size_t vstride = 0, DeviceBuffer *work = nullptr, const uint32_t *forms = nullptr);
 
 // One axis of length n (a prime factor above 7) as a Bluestein transform, in
 // chunks of padded lines of at most 256 MB held in `work`.
@@ -637,7 +699,7 @@ int bluestein_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, u
 // Lengths with a prime factor above 7 use `work` (default: the device's main
 // scratch, for callers holding the context lock).
 int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
-             int first, int last, size_t vstride, DeviceBuffer *work) {
+             int first, int last, size_t vstride, DeviceBuffer *work, const uint32_t *forms) {
   const size_t nvox = vstride ? vstride : size_t(nx) * ny * nz;
   const uint32_t dims[3] = {nx, ny, nz};
   for (int axis = first; axis <= last; ++axis) {
@@ -648,7 +710,7 @@ int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_
       continue;
     }
     if (n == 128 || n == 256 || n == 512 || n == 1024) {
-      CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st, nvox));
+      CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st, nvox, forms ? forms[axis] : kFormAuto));
       continue;
     }
     if (axis > 0 && (n == 8 || n == 16 || n == 32 || n == 64) && count <= 65535) {
@@ -1236,10 +1298,113 @@ struct SlabUpload {
   }
 };
 
+// Fields of planes [z0, z1) and their x pass: fused (k_build_fields_rows) or
+// the separate build and row pass.
+int build_fields_x(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan &pl, FieldParams fp, uint32_t z0,
+                   uint32_t z1, bool fused, const float2 *twx, cudaStream_t st) {
+  const uint32_t npk = pl.npk;
+  float2 *spec = sc.spec.as<float2>();
+  int sms = 0;
+  CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  fp.i0 = size_t(z0) * pl.npix, fp.i1 = size_t(z1) * pl.npix;
+  if (fused) {
+    const size_t smem = fields_rows_smem(pl.nx, npk);
+    const uint32_t rows = (z1 - z0) * pl.ny;
+    int per_sm = 1;
+    auto launch = [&](auto kern) -> int {
+      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
+      const unsigned grid = unsigned(std::min<size_t>(rows, size_t(std::max(1, per_sm)) * sms));
+      kern<<<grid, 256, smem, st>>>(fp, twx, npk);
+      return CYR_OK;
+    };
+    const int slot = ctx.prof.begin(kBuildFieldsRows, st);
+    const bool euler = o->morphology_type == 0;
+    if (pl.nx == 128) CYR_TRY(launch(euler ? k_build_fields_rows<0, 4> : k_build_fields_rows<1, 4>));
+    if (pl.nx == 256) CYR_TRY(launch(euler ? k_build_fields_rows<0, 8> : k_build_fields_rows<1, 8>));
+    if (pl.nx == 512) CYR_TRY(launch(euler ? k_build_fields_rows<0, 16> : k_build_fields_rows<1, 16>));
+    if (pl.nx == 1024) CYR_TRY(launch(euler ? k_build_fields_rows<0, 32> : k_build_fields_rows<1, 32>));
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+    return CYR_OK;
+  }
+  const uint32_t blocks = uint32_t(std::min<size_t>((fp.i1 - fp.i0 + 255) / 256, size_t(sms) * 8));
+  const int slot = ctx.prof.begin(kBuildFields, st);
+  if (o->morphology_type == 0)
+    k_build_fields<0><<<blocks, 256, 0, st>>>(fp);
+  else
+    k_build_fields<1><<<blocks, 256, 0, st>>>(fp);
+  ctx.prof.end(slot, st);
+  CYR_CUDA(cudaGetLastError());
+  return fft_axes(ctx, spec + fp.i0, pl.nx, pl.ny, z1 - z0, npk, st, 0, 0, pl.nvox, &sc.blue);
+}
+
+// Autotuning of the FIELDS transform for one shape (the first device-resident
+// request of it on this device): the fused or separate build + x pass and the
+// launch form of the y and z passes are each timed once on the packed-field
+// buffer, before the build overwrites every element of it, and the fastest
+// kept.  Every candidate computes the same numbers.
+int tune_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan &pl, const FieldParams &fp,
+                bool fused_ok, const float2 *twx, cudaStream_t st, DeviceContext::FieldTune &ft) {
+  struct Cand {
+    int kind;  // 0 build + x, 1 y pass, 2 z pass
+    uint32_t choice;
+    cudaEvent_t a, b;
+  };
+  std::vector<Cand> cands;
+  if (fused_ok) cands.push_back({0, 1, nullptr, nullptr}), cands.push_back({0, 0, nullptr, nullptr});
+  const uint32_t dims[3] = {pl.nx, pl.ny, pl.nz};
+  for (int axis = 1; axis <= 2; ++axis) {
+    const std::vector<uint32_t> f = column_forms(ctx, dims[axis], pl.nx);
+    if (f.size() > 1)
+      for (uint32_t v : f) cands.push_back({axis, v, nullptr, nullptr});
+  }
+  ft.fused = fused_ok;
+  if (cands.empty()) return CYR_OK;
+  for (Cand &c : cands) {
+    CYR_CUDA(cudaEventCreate(&c.a));
+    CYR_CUDA(cudaEventCreate(&c.b));
+  }
+  int rc = CYR_OK;
+  for (Cand &c : cands) {
+    CYR_CUDA(cudaEventRecord(c.a, st));
+    if (c.kind == 0)
+      rc = build_fields_x(ctx, sc, o, pl, fp, 0, pl.nz, c.choice == 1, twx, st);
+    else
+      rc = warp_fft_pass(ctx, sc.spec.as<float2>(), pl.nx, pl.ny, pl.nz, pl.npk, c.kind, st, pl.nvox, c.choice);
+    if (rc != CYR_OK) break;
+    CYR_CUDA(cudaEventRecord(c.b, st));
+  }
+  if (rc == CYR_OK) {
+    CYR_CUDA(cudaEventSynchronize(cands.back().b));
+    float best[3] = {1e30f, 1e30f, 1e30f};
+    std::string rep[3];
+    for (Cand &c : cands) {
+      float ms = 0.f;
+      CYR_CUDA(cudaEventElapsedTime(&ms, c.a, c.b));
+      char buf[64];
+      std::snprintf(buf, sizeof buf, " %s %.3f ms",
+                    c.kind == 0 ? (c.choice ? "fused" : "separate") : form_name(c.choice), ms);
+      rep[c.kind] += buf;
+      if (ms < best[c.kind]) {
+        best[c.kind] = ms;
+        if (c.kind == 0)
+          ft.fused = c.choice == 1;
+        else
+          ft.form[c.kind] = c.choice;
+      }
+    }
+    ft.report = "build+x:" + (rep[0].empty() ? std::string(" -") : rep[0]) + "; y:" +
+                (rep[1].empty() ? std::string(" -") : rep[1]) + "; z:" + (rep[2].empty() ? std::string(" -") : rep[2]);
+  }
+  for (Cand &c : cands) cudaEventDestroy(c.a), cudaEventDestroy(c.b);
+  return rc;
+}
+
 // FIELDS strategy after the moments: field means, packed field spectra, then
 // every energy (in batches) and k from them.
 int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan &pl, const unsigned char *dp,
-               const float4 *d_vox, float *d_out, cudaStream_t st, size_t nsamp, const SlabUpload *up) {
+               const float4 *d_vox, float *d_out, cudaStream_t st, size_t nsamp, const SlabUpload *up,
+               bool capturing) {
   const uint32_t npk = pl.npk;
   CYR_TRY(sc.spec.ensure(size_t(npk) * pl.nvox * sizeof(float2)));
   CYR_TRY(sc.images.ensure(image_bytes(pl, pl.ebatch)));
@@ -1257,8 +1422,30 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
     fp.hann_z = reinterpret_cast<const float *>(dp + pl.off_hz);
   }
   fp.out = spec;
-  int sms = 0;
-  CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  // the field build fused with the x pass when x is a warp-FFT length and the row's lines fit
+  const bool fused_ok = (pl.nx == 128 || pl.nx == 256 || pl.nx == 512 || pl.nx == 1024) &&
+                        fields_rows_smem(pl.nx, npk) <= kFftSmemBudget;
+  const float2 *twx = nullptr;
+  if (fused_ok) CYR_TRY(get_twiddles(ctx, pl.nx, &twx));
+  // tuned launch forms of this shape, tuned here on its first device-resident request
+  char key[96];
+  std::snprintf(key, sizeof key, "%u,%u,%u,%u", pl.nx, pl.ny, pl.nz, npk);
+  DeviceContext::FieldTune ft;
+  bool have = false;
+  {
+    std::lock_guard<std::mutex> lk(ctx.tables_mu);
+    auto it = ctx.ftune.find(key);
+    if (it != ctx.ftune.end()) ft = it->second, have = true;
+  }
+  if (!have) {
+    ft.fused = fused_ok;
+    if (ctx.autotune && !up && !capturing && !ctx.prof.active) {
+      CYR_TRY(tune_fields(ctx, sc, o, pl, fp, fused_ok, twx, st, ft));
+      std::lock_guard<std::mutex> lk(ctx.tables_mu);
+      ctx.ftune[key] = ft;
+    }
+  }
+  const bool fused = fused_ok && ft.fused;
   // fields of planes [z0, z1), then their x and y passes (the axes commute; z comes last)
   const uint32_t step = up ? up->planes : pl.nz, nslab = up ? up->count : 1;
   for (uint32_t sl = 0; sl < nslab; ++sl) {
@@ -1267,19 +1454,12 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
       CYR_TRY(const_cast<SlabUpload *>(up)->issue(sl));
       CYR_CUDA(cudaStreamWaitEvent(st, up->events[sl], 0));
     }
-    fp.i0 = size_t(z0) * pl.npix, fp.i1 = size_t(z1) * pl.npix;
-    const uint32_t blocks = uint32_t(std::min<size_t>((fp.i1 - fp.i0 + 255) / 256, size_t(sms) * 8));
-    int slot = ctx.prof.begin(kBuildFields, st);
-    if (o->morphology_type == 0)
-      k_build_fields<0><<<blocks, 256, 0, st>>>(fp);
-    else
-      k_build_fields<1><<<blocks, 256, 0, st>>>(fp);
-    ctx.prof.end(slot, st);
-    CYR_CUDA(cudaGetLastError());
-    CYR_TRY(fft_axes(ctx, spec + fp.i0, pl.nx, pl.ny, z1 - z0, npk, st, 0, 1, pl.nvox, &sc.blue));
+    CYR_TRY(build_fields_x(ctx, sc, o, pl, fp, z0, z1, fused, twx, st));
+    CYR_TRY(fft_axes(ctx, spec + size_t(z0) * pl.npix, pl.nx, pl.ny, z1 - z0, npk, st, 1, 1, pl.nvox, &sc.blue,
+                     ft.form));
     if (up) CYR_TRY(const_cast<SlabUpload *>(up)->issue(sl + 1));  // the next slab's copy, behind this slab's kernels
   }
-  CYR_TRY(fft_axes(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st, 2, 2, 0, &sc.blue));
+  CYR_TRY(fft_axes(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st, 2, 2, 0, &sc.blue, ft.form));
   // bin 0 of each packed volume replaced by the mean of its neighbours
   CYR_TRY(sc.dc.ensure(size_t(kMaxPacked) * sizeof(float2)));
   int slot = ctx.prof.begin(kDc, st);
@@ -1496,7 +1676,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
     CYR_CUDA(cudaGetLastError());
     if (pl.fields) {
       const size_t nsamp = pl.npix * ((mp.nz + mp.zstep - 1) / mp.zstep);
-      CYR_TRY(run_fields(ctx, sc, o, pl, dp, d_vox, d_out, st, nsamp, slabs ? &upload : nullptr));
+      CYR_TRY(run_fields(ctx, sc, o, pl, dp, d_vox, d_out, st, nsamp, slabs ? &upload : nullptr, mode.capturing));
       // an event recorded inside a capture cannot be waited on outside it (slots keep order by their stream)
       if (!mode.capturing) CYR_CUDA(cudaEventRecord(sc.last_use, st));
       return CYR_OK;
@@ -2340,6 +2520,11 @@ int cyr_tuning_report(char *buf, size_t len) {
                   kv.second.stage ? 1 : 0, kv.second.tx, kv.second.ms);
     r += line;
   }
+  for (const auto &kv : ctx->ftune) {
+    if (kv.second.report.empty()) continue;
+    r += "fields[" + kv.first + "]: build+x=" + (kv.second.fused ? "fused" : "separate") +
+         " y=" + form_name(kv.second.form[1]) + " z=" + form_name(kv.second.form[2]) + " (" + kv.second.report + ")\n";
+  }
   if (buf && len) {
     std::strncpy(buf, r.c_str(), len - 1);
     buf[len - 1] = 0;
@@ -2455,6 +2640,7 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
   CYR_TRY(get_context(&ctx));
   std::lock_guard<std::mutex> lk(ctx->mu);
   CYR_TRY(setup_attrs(*ctx));
+  CYR_TRY(ctx->main.init());  // the scratch's completion event (this may be the process's first call)
   const size_t vox_bytes = pl.nvox * pl.nmat * sizeof(float4);
   CYR_TRY(ctx->vox_in.ensure(vox_bytes));
   CYR_TRY(ctx->main.spec.ensure(3 * pl.nvox * sizeof(float2)));
@@ -2463,9 +2649,13 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
   CYR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   int rc = CYR_OK;
   do {
-    cudaStreamWaitEvent(st, ctx->main.last_use, 0);
-    cudaMemcpyAsync(ctx->main.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(ctx->vox_in.ptr, voxels, vox_bytes, cudaMemcpyHostToDevice, st);
+    if (cudaStreamWaitEvent(st, ctx->main.last_use, 0) != cudaSuccess ||
+        cudaMemcpyAsync(ctx->main.params.ptr, pl.arena.data(), pl.arena.size(), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(ctx->vox_in.ptr, voxels, vox_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "polarization upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
     const unsigned char *dp = ctx->main.params.as<unsigned char>();
     BuildParams bp{};
     bp.vox = ctx->vox_in.as<float4>();
@@ -2491,8 +2681,9 @@ int cyr_compute_polarization(const cyr_options *opt, const float *optical, const
       k_build<0, false><<<blocks, 256, 0, st>>>(bp, mce);
     else
       k_build<1, false><<<blocks, 256, 0, st>>>(bp, mce);
-    if (cudaGetLastError() != cudaSuccess) {
-      rc = fail(CYR_ERR_CUDA, "polarization kernel launch failed");
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) {
+      rc = fail(CYR_ERR_CUDA, "polarization kernel launch failed: %s", cudaGetErrorString(le));
       break;
     }
     const size_t cb = pl.nvox * sizeof(float2);

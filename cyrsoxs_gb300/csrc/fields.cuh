@@ -120,6 +120,90 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
   }
 }
 
+// Field build fused with the x-row FFT (rows of N = 32 V points): a block owns
+// one row (y, z) at a time and writes the row's packed fields into swizzled
+// shared-memory lines, [npk][N] (the same fields, windowing and means as
+// k_build_fields); each warp then loads a line into registers, runs the warp
+// FFT with that line as its exchange buffer, and stores the transformed row.
+// The packed volumes leave the chip once, already x-transformed: the build's
+// write and the row pass's read-back of 8 npk bytes per voxel are gone.
+// Shared memory: (npk + 1) N float2 (lines and twiddles).
+template <int MORPH, int V>
+__global__ void __launch_bounds__(256) k_build_fields_rows(FieldParams p, const float2 *__restrict__ tw_n,
+                                                           uint32_t npk) {
+  constexpr uint32_t N = 32 * V;
+  extern __shared__ float2 fsm[];
+  float2 *tws = fsm;        // the warp FFT's stage twiddles (N - radix entries)
+  float2 *lines = fsm + N;  // [npk][N]: element x of line j at lines[j N + swz(x)]
+  __shared__ float mean[kMaxFields];
+  field_means(p.mom, p.nmat, p.nsamp, mean);
+  warp_twiddles<V>(tws, tw_n);
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const uint32_t nrows = uint32_t((p.i1 - p.i0) / N);
+  for (uint32_t r = blockIdx.x; r < nrows; r += gridDim.x) {
+    __syncthreads();  // means and twiddles ready; the previous row's lines consumed
+    const size_t rowbase = p.i0 + size_t(r) * N;
+    const uint32_t y = uint32_t((rowbase / N) % p.ny), z = uint32_t(rowbase / (size_t(N) * p.ny));
+    const float wyz = p.hann_x ? p.hann_y[y] * p.hann_z[z] : 1.f;
+    for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+      const size_t i = rowbase + x;
+      const float w = p.hann_x ? p.hann_x[x] * wyz : 1.f;
+      float2 *o = lines + swz(x);
+      float T = 0.f, pend = 0.f;
+      uint32_t g = 0;
+      auto emit = [&](float v) {
+        v -= mean[g];
+        if (g & 1u)
+          o[(g >> 1) * N] = make_float2(pend, v);
+        else
+          pend = v;
+        ++g;
+      };
+      for (uint32_t m0 = 0; m0 < p.nmat; m0 += 4) {
+        float4 sv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (m0 + u < p.nmat) sv[u] = __ldg(&p.vox[(m0 + u) * p.nvox + i]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (m0 + u >= p.nmat) break;
+          float sx, sy, sz, pa, pui;
+          director<MORPH>(sv[u], sx, sy, sz, pa, pui);
+          const float wa = w * pa;
+          const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
+          T += f0 + f1 + f2 + f6;
+          emit(f0);
+          emit(f1);
+          emit(f2);
+          emit(wa * sx * sy);
+          emit(wa * sx * sz);
+          emit(wa * sy * sz);
+          emit(f6);
+        }
+      }
+      emit(T);
+      if (g & 1u) o[(g >> 1) * N] = make_float2(pend, 0.f);
+    }
+    __syncthreads();
+    for (uint32_t j = warp; j < npk; j += nw) {
+      float2 *line = lines + j * N;
+      float2 v[V];
+      const uint32_t lx = swz(lane);
+#pragma unroll
+      for (int k = 0; k < V; ++k) v[k] = line[V >= 16 ? swz_at(lx, k) : swz(lane + 32 * k)];
+      __syncwarp();
+      warp_fft<V>(v, line, tws, lane);
+      float2 *dst = p.out + size_t(j) * p.nvox + rowbase;
+#pragma unroll
+      for (int k = 0; k < V; ++k) dst[lane + 32 * k] = v[k];
+    }
+  }
+}
+
+__host__ __device__ constexpr size_t fields_rows_smem(uint32_t n, uint32_t npk) {
+  return size_t(npk + 1) * n * sizeof(float2);
+}
+
 // Ewald projection from the packed field spectra, for a batch of energies
 // (blockIdx.y) and every E angle.  Per energy the unpacking and combination
 // coefficients of tensor entry v (xx xy xz yy yz zz) and packed volume j are

@@ -61,6 +61,8 @@ def rel_err(a, ref, thr=1e-6):
                                          # TMA column passes: 32-column tiles, 16-column tiles (nx not a
                                          # multiple of 32), 512-point lines on several volumes
                                          ((4, 256, 64), 2), ((256, 4, 48), 1), ((2, 256, 80), 2), ((2, 512, 16), 3),
+                                         # TMA column passes on 128-point lines (16- and 32-column tiles)
+                                         ((128, 8, 48), 1), ((4, 128, 64), 2), ((128, 4, 32), 3),
                                          # Bluestein: lengths with a prime factor above 7 on every axis
                                          ((3, 11, 13), 2), ((2, 97, 101), 1), ((61, 6, 40), 1), ((2, 4, 2039), 1),
                                          ((17, 256, 48), 1), ((5, 127, 64), 2), ((1, 22, 1031), 1)])
@@ -213,6 +215,28 @@ PRIME = [
 def test_prime_lengths_match_oracle(case, strategy):
     nat = native()
     got = nat.cuda_main(options_for(case, strategy=strategy), cases.optical_constants(case),
+                        cases.voxels(case)).astype(np.float64)
+    want = oracle.run_case(case)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    e = rel_err(got, want)
+    assert e.max() <= TOL, e.max()
+
+
+# The field build fused with the x-row FFT (k_build_fields_rows) for every warp-FFT row length, Euler and vector
+# morphologies, windowed and not, with 2 to 5 materials (up to 18 packed volumes in shared memory).
+FUSED_ROWS = [
+    cases.Case("rows128_vector_hann", 128, 128, 8, 3, [284.0, 286.0], seed=71, morphology=cases.VECTOR, windowing=1,
+               geometry="blobs", angles=(0.0, 120.0, 60.0)),
+    cases.Case("rows512_euler", 512, 512, 4, 2, [285.0], seed=72, geometry="blobs", angles=(0.0, 90.0, 45.0)),
+    cases.Case("rows1024_euler_mask", 1024, 1024, 4, 5, [283.0], seed=73, geometry="blobs", rot_mask=1,
+               angles=(0.0, 150.0, 75.0)),
+]
+
+
+@pytest.mark.parametrize("case", FUSED_ROWS, ids=[c.name for c in FUSED_ROWS])
+def test_fused_field_rows_match_oracle(case):
+    nat = native()
+    got = nat.cuda_main(options_for(case, strategy=2), cases.optical_constants(case),
                         cases.voxels(case)).astype(np.float64)
     want = oracle.run_case(case)
     assert np.array_equal(np.isnan(got), np.isnan(want))

@@ -124,12 +124,12 @@ def test_device_buffers():
 
 def test_invalid_request_is_rejected_at_submit():
     torch, nat, serving = _setup()
-    bad = nat.Options(nx=22, ny=8, nz=4, num_material=1, energies=[285.0], start_angle=0, end_angle=0,
-                      increment_angle=0, phys_size=5.0)
+    bad = nat.Options(nx=4099, ny=2, nz=1, num_material=1, energies=[285.0], start_angle=0, end_angle=0,
+                      increment_angle=0, phys_size=5.0)  # prime, beyond the Bluestein limit
     with serving.Server(slots=1) as srv:
         with pytest.raises(nat.CyrError):
-            srv.submit(bad, np.zeros((1, 1, 4), np.float32), np.zeros((1, 4, 8, 22, 4), np.float32),
-                       np.zeros((1, 1, 8, 22), np.float32))
+            srv.submit(bad, np.zeros((1, 1, 4), np.float32), np.zeros((1, 1, 2, 4099, 4), np.float32),
+                       np.zeros((1, 1, 2, 4099), np.float32))
 
 
 def test_one_slot_alternating_signatures_after_a_capture():
