@@ -129,8 +129,8 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
 // write and the row pass's read-back of 8 npk bytes per voxel are gone.
 // Shared memory: (npk + 1) N float2 (lines and twiddles).
 template <int MORPH, int V>
-__global__ void __launch_bounds__(256) k_build_fields_rows(FieldParams p, const float2 *__restrict__ tw_n,
-                                                           uint32_t npk) {
+__global__ void __launch_bounds__(256, V <= 16 ? 3 : 1) k_build_fields_rows(FieldParams p, const float2 *__restrict__ tw_n,
+                                                                            uint32_t npk) {
   constexpr uint32_t N = 32 * V;
   extern __shared__ float2 fsm[];
   float2 *tws = fsm;        // the warp FFT's stage twiddles (N - radix entries)
