@@ -69,6 +69,7 @@ def parse():
     ap.add_argument("--skip-fp64", action="store_true", help="skip the comparison with the on-GPU FP64 pipeline")
     ap.add_argument("--served-only", action="store_true", help="only the batched and serving measurements")
     ap.add_argument("--slots", type=int, default=8, help="serving slots (requests in flight)")
+    ap.add_argument("--no-groups", action="store_true", help="serve without request groups (one launch per request)")
     ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--served-reps", type=int, default=5, help="timed passes per batched mode (median reported)")
     return ap.parse_args()
@@ -540,7 +541,8 @@ def served_benchmarks(args):
     all submitted at t = 0, device-resident (plain = cyr_simulate_device and a
     synchronisation per request, in order) and again from pinned host memory
     (plain = cyr_cuda_main per request); served = the serving engine
-    (continuous batching over `--slots` slots, CUDA graphs).
+    (continuous batching over `--slots` slots, CUDA graphs, and request groups:
+    queued same-shape requests on device buffers share one launch per kernel).
     serving: a seeded Poisson stream (200 requests/s) of requests of random
     size, materials, energies and angles with device-resident morphologies;
     plain = the same arrivals served one at a time in arrival order.  Each
@@ -603,7 +605,7 @@ def served_benchmarks(args):
                                                             "(host<->device copies inside the timed region)")):
         plain_batch(host)
         tp, lp, tpa = _median_pass(lambda: plain_batch(host), args.served_reps)
-        with serving.Server(slots=args.slots, graphs=True) as srv:
+        with serving.Server(slots=args.slots, graphs=True, groups=not args.no_groups) as srv:
             served_batch(srv, host)
             ts, ls, tsa = _median_pass(lambda: served_batch(srv, host), args.served_reps)
             st = srv.stats()
@@ -614,8 +616,9 @@ def served_benchmarks(args):
             "passes": len(tpa),
             "plain": {"patterns_per_s": patterns / tp, "seconds": tp, "pass_seconds": tpa, **_lat_summary(lp)},
             "served": {"patterns_per_s": patterns / ts, "seconds": ts, "pass_seconds": tsa, "slots": args.slots,
-                       "graphs": True,
+                       "graphs": True, "groups": not args.no_groups,
                        "graph_replays": st["graph_replays"], "graph_captures": st["graph_captures"],
+                       "group_runs": st["group_runs"], "grouped_requests": st["grouped_requests"],
                        **_lat_summary(ls)},
             "speedup": tp / ts,
         }
@@ -669,9 +672,10 @@ def served_benchmarks(args):
 
     plain_stream()
     tps, lps = plain_stream()
-    with serving.Server(slots=args.slots) as srv:
+    with serving.Server(slots=args.slots, groups=not args.no_groups) as srv:
         served_stream(srv)
         tss, lss = served_stream(srv)
+        sst = srv.stats()
     mean_vox = sum(r[3].numel() // 4 for r in stream_reqs) / len(stream_reqs)
     out["serving"] = {
         "config": f"{len(stream_reqs)} requests, Poisson arrivals at 200/s (seeded); volume log-uniform in "
@@ -680,7 +684,8 @@ def served_benchmarks(args):
                   f"{len(shared_vox)} distinct shapes, requests of one shape share its morphology)",
         "requests": len(stream_reqs), "patterns": spat, "arrival_span_s": stream_reqs[-1][0],
         "plain": {"patterns_per_s": spat / tps, "seconds": tps, **_lat_summary(lps)},
-        "served": {"patterns_per_s": spat / tss, "seconds": tss, "slots": args.slots, **_lat_summary(lss)},
+        "served": {"patterns_per_s": spat / tss, "seconds": tss, "slots": args.slots, "groups": not args.no_groups,
+                   "group_runs": sst["group_runs"], "grouped_requests": sst["grouped_requests"], **_lat_summary(lss)},
         "speedup": tps / tss,
     }
     del stream_reqs, shared_vox

@@ -2191,6 +2191,7 @@ struct ServerRequest {
   float *d_out = nullptr;
   size_t vox_bytes = 0, out_bytes = 0, footprint = 0;
   std::string key;  // graph signature
+  std::string group_key;  // requests with the same key may share launches (empty: never grouped)
   Plan plan;        // host plan (strategy resolved), made once at submit
   double work = 0;  // share of the GPU the request fills (1 = saturating)
   int status = -1;  // -1 queued or running, else a CYR_* code
@@ -2212,6 +2213,7 @@ struct Slot {
   size_t host_arena_bytes = 0;
   unsigned *host_errors = nullptr;  // pinned copy of the request's device error counter
   std::shared_ptr<ServerRequest> req;
+  std::vector<std::shared_ptr<ServerRequest>> group;  // the other requests sharing req's launches
   std::map<std::string, GraphEntry> graphs;
   std::map<std::string, uint64_t> warm;  // signature -> scratch generation after its last uncaptured run
   uint64_t generation() const { return sc.generation; }
@@ -2224,13 +2226,14 @@ struct Server {
   size_t budget = 0, in_use = 0;
   double inflight_work = 0;
   bool graphs = false;
+  bool groups = false;  // same-shape queued requests share one launch per kernel
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<std::shared_ptr<ServerRequest>> queue;
   std::map<uint64_t, std::shared_ptr<ServerRequest>> requests;
   uint64_t next_id = 1;
   bool stop = false;
-  std::atomic<uint64_t> completed{0}, failed{0}, replays{0}, captures{0};
+  std::atomic<uint64_t> completed{0}, failed{0}, replays{0}, captures{0}, group_runs{0}, grouped{0};
   std::thread worker;
 };
 
@@ -2260,6 +2263,250 @@ int plan_request(ServerRequest &r, bool staged) {
   r.key = head;
   for (float e : r.energies) r.key += std::to_string(e) + ",";
   for (float k : r.kvecs) r.key += std::to_string(k) + ",";
+  // requests that can share launches: FIELDS, LAB frame, k along z, device buffers; all but the
+  // morphology, the energies and the optical constants equal
+  r.group_key.clear();
+  if (pl.fields && !pl.material_frame && r.opt.case_type == 0 && pl.nk == 1 && pl.nbasis == 2 && r.d_vox) {
+    char g[256];
+    std::snprintf(g, sizeof g, "%u,%u,%u,%u,%u,%a,%a,%a,%a,%u,%u,%u,%u,%u", r.opt.nx, r.opt.ny, r.opt.nz,
+                  r.opt.num_material, r.opt.num_energies, double(r.opt.start_angle), double(r.opt.end_angle),
+                  double(r.opt.increment_angle), double(r.opt.phys_size), r.opt.morphology_type,
+                  r.opt.ewald_interpolation, pl.hanning ? 1u : 0u, r.opt.rot_mask, pl.has_rows ? 1u : 0u);
+    r.group_key = g;
+  }
+  return CYR_OK;
+}
+
+// Grows the slot's pinned copy of the parameter arena (its graphs read the old one: dropped).
+int ensure_host_arena(Slot &sl, size_t bytes) {
+  if (bytes <= sl.host_arena_bytes) return CYR_OK;
+  if (sl.host_arena) {
+    CYR_CUDA(cudaStreamSynchronize(sl.stream));
+    cudaFreeHost(sl.host_arena);
+    sl.host_arena = nullptr;
+  }
+  for (auto &kv : sl.graphs) cudaGraphExecDestroy(kv.second.exec);
+  sl.graphs.clear();
+  sl.host_arena_bytes = std::max<size_t>(bytes, 64 * 1024);
+  CYR_CUDA(cudaMallocHost(&sl.host_arena, sl.host_arena_bytes));
+  return CYR_OK;
+}
+
+// Requests per group: at most 16, and their packed volumes must fit one DC block.
+constexpr uint32_t kMaxGroup = 16;
+
+// A group of same-key requests (FIELDS strategy) with one launch per kernel:
+// moments, field build + x pass, y and z passes over all G npk packed volumes,
+// DC, then the Ewald projection, rotation and detector warp over the G E
+// "virtual energies" (request q's energy e is virtual energy q E + e), each
+// request's constants in per-virtual-energy tables.  Every request computes
+// exactly what it computes alone (same kernels, same arithmetic per element).
+int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerRequest>> &g) {
+  DeviceContext &ctx = *S.ctx;
+  Scratch &sc = sl.sc;
+  cudaStream_t st = sl.stream;
+  const ServerRequest &r0 = *g[0];
+  const Plan &p0 = r0.plan;
+  const cyr_options *o = &r0.opt;
+  const uint32_t G = uint32_t(g.size()), E = p0.ne, npk = p0.npk, nmat = p0.nmat;
+  const int W = int(p0.ny), H = int(p0.nx);  // the reference hands NPP width = Ny, height = Nx
+  CYR_TRY(setup_attrs(ctx));
+  CYR_TRY(sc.init());
+  // arena: request 0's (the shared geometry tables), then the per-virtual-energy and pointer tables
+  std::vector<unsigned char> arena = p0.arena;
+  std::vector<float4> fc;
+  std::vector<float> km;
+  std::vector<int2> rows;
+  std::vector<const float4 *> vp;
+  std::vector<float *> op;
+  for (const auto &r : g) {
+    const Plan &pl = r->plan;
+    const float4 *c = reinterpret_cast<const float4 *>(pl.arena.data() + pl.off_fcoef);
+    fc.insert(fc.end(), c, c + size_t(E) * 6 * npk);
+    const float *k = reinterpret_cast<const float *>(pl.arena.data() + pl.off_kmag);
+    km.insert(km.end(), k, k + E);
+    if (p0.has_rows) {
+      const int2 *rw = reinterpret_cast<const int2 *>(pl.arena.data() + pl.off_rows);
+      rows.insert(rows.end(), rw, rw + size_t(E) * H);
+    }
+    vp.push_back(r->d_vox);
+    op.push_back(r->d_out);
+  }
+  const size_t off_c = arena_put(arena, fc.data(), fc.size());
+  const size_t off_k = arena_put(arena, km.data(), km.size());
+  const size_t off_r = p0.has_rows ? arena_put(arena, rows.data(), rows.size()) : 0;
+  const size_t off_v = arena_put(arena, vp.data(), vp.size());
+  const size_t off_o = arena_put(arena, op.data(), op.size());
+  arena.resize((arena.size() + 255) & ~size_t(255));
+  CYR_TRY(ensure_host_arena(sl, arena.size()));
+  std::memcpy(sl.host_arena, arena.data(), arena.size());
+  CYR_TRY(sc.params.ensure(arena.size()));
+  CYR_CUDA(cudaMemcpyAsync(sc.params.ptr, sl.host_arena, arena.size(), cudaMemcpyHostToDevice, st));
+  const unsigned char *dp = sc.params.as<unsigned char>();
+  // scratch; virtual energies per Ewald / rotation launch: whole records, at most 256 MB of them
+  const size_t nvox = p0.nvox, npix = p0.npix;
+  const uint32_t nep = gram_nep(p0), total = G * E;
+  uint32_t vb = std::min<uint32_t>(total, 512);
+  while (vb > nep && image_bytes(p0, vb) > (size_t(256) << 20)) vb -= nep;
+  if (vb < total) vb = std::max(nep, vb / nep * nep);
+  CYR_TRY(sc.spec.ensure(size_t(G) * npk * nvox * sizeof(float2)));
+  CYR_TRY(sc.images.ensure(image_bytes(p0, vb)));
+  CYR_TRY(sc.avg.ensure(size_t(vb) * npix * sizeof(float)));
+  CYR_TRY(sc.moments.ensure(size_t(G) * nmat * kMoments * sizeof(double)));
+  CYR_TRY(sc.dc.ensure(size_t(G) * npk * sizeof(float2)));
+  CYR_TRY(sc.errors.ensure(sizeof(unsigned)));
+  CYR_CUDA(cudaMemsetAsync(sc.errors.ptr, 0, sizeof(unsigned), st));
+  CYR_CUDA(cudaMemsetAsync(sc.moments.ptr, 0, size_t(G) * nmat * kMoments * sizeof(double), st));
+  float2 *spec = sc.spec.as<float2>();
+  int sms = 0;
+  CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  const float4 *const *vox_g = reinterpret_cast<const float4 *const *>(dp + off_v);
+  // moments of every request (blockIdx.z = request), over the z-plane subsample
+  MomentParams mp{};
+  mp.vox_g = vox_g;
+  mp.nx = p0.nx, mp.ny = p0.ny, mp.nz = p0.nz, mp.nmat = nmat;
+  mp.nvox = nvox;
+  if (p0.hanning) {
+    mp.hann_x = reinterpret_cast<const float *>(dp + p0.off_hx);
+    mp.hann_y = reinterpret_cast<const float *>(dp + p0.off_hy);
+    mp.hann_z = reinterpret_cast<const float *>(dp + p0.off_hz);
+  }
+  mp.out = sc.moments.as<double>();
+  mp.zstep = p0.mom_zstep;
+  const size_t nsamp = npix * ((p0.nz + mp.zstep - 1) / mp.zstep);
+  {
+    const dim3 grid(uint32_t(std::max<size_t>(1, std::min<size_t>((nsamp + 2047) / 2048, size_t(sms) * 4))), nmat, G);
+    const int slot = ctx.prof.begin(kMom, st);
+    if (o->morphology_type == 0)
+      k_moments<0><<<grid, 256, 0, st>>>(mp);
+    else
+      k_moments<1><<<grid, 256, 0, st>>>(mp);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+  }
+  // field build + x pass (blockIdx.y = request), then y and z over all G npk volumes
+  FieldParams fp{};
+  fp.vox_g = vox_g;
+  fp.nx = p0.nx, fp.ny = p0.ny, fp.nz = p0.nz, fp.nmat = nmat;
+  fp.nvox = nvox;
+  fp.mom = sc.moments.as<double>();
+  fp.mom_stride = size_t(nmat) * kMoments;
+  fp.nsamp = nsamp;
+  fp.out = spec;
+  fp.out_stride = size_t(npk) * nvox;
+  fp.i0 = 0, fp.i1 = nvox;
+  if (p0.hanning) fp.hann_x = mp.hann_x, fp.hann_y = mp.hann_y, fp.hann_z = mp.hann_z;
+  const bool fused_ok = (p0.nx == 128 || p0.nx == 256 || p0.nx == 512 || p0.nx == 1024) &&
+                        fields_rows_smem(p0.nx, npk) <= kFftSmemBudget;
+  DeviceContext::FieldTune ft;
+  {
+    char key[96];
+    std::snprintf(key, sizeof key, "%u,%u,%u,%u", p0.nx, p0.ny, p0.nz, npk);
+    std::lock_guard<std::mutex> lk(ctx.tables_mu);
+    auto it = ctx.ftune.find(key);
+    if (it != ctx.ftune.end()) ft = it->second;
+  }
+  if (fused_ok && ft.fused) {
+    const float2 *twx = nullptr;
+    CYR_TRY(get_twiddles(ctx, p0.nx, &twx));
+    const size_t smem = fields_rows_smem(p0.nx, npk);
+    const uint32_t rws = p0.nz * p0.ny;
+    int per_sm = 1;
+    auto launch = [&](auto kern) -> int {
+      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
+      const size_t want = (size_t(std::max(1, per_sm)) * sms + G - 1) / G;
+      kern<<<dim3(unsigned(std::min<size_t>(rws, want)), G), 256, smem, st>>>(fp, twx, npk);
+      return CYR_OK;
+    };
+    const int slot = ctx.prof.begin(kBuildFieldsRows, st);
+    const bool euler = o->morphology_type == 0;
+    if (p0.nx == 128) CYR_TRY(launch(euler ? k_build_fields_rows<0, 4> : k_build_fields_rows<1, 4>));
+    if (p0.nx == 256) CYR_TRY(launch(euler ? k_build_fields_rows<0, 8> : k_build_fields_rows<1, 8>));
+    if (p0.nx == 512) CYR_TRY(launch(euler ? k_build_fields_rows<0, 16> : k_build_fields_rows<1, 16>));
+    if (p0.nx == 1024) CYR_TRY(launch(euler ? k_build_fields_rows<0, 32> : k_build_fields_rows<1, 32>));
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+  } else {
+    const uint32_t blocks =
+        uint32_t(std::max<size_t>(1, std::min<size_t>((nvox + 255) / 256, (size_t(sms) * 8 + G - 1) / G)));
+    const int slot = ctx.prof.begin(kBuildFields, st);
+    if (o->morphology_type == 0)
+      k_build_fields<0><<<dim3(blocks, G), 256, 0, st>>>(fp);
+    else
+      k_build_fields<1><<<dim3(blocks, G), 256, 0, st>>>(fp);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+    CYR_TRY(fft_axes(ctx, spec, p0.nx, p0.ny, p0.nz, npk * G, st, 0, 0, 0, &sc.blue, ft.form));
+  }
+  CYR_TRY(fft_axes(ctx, spec, p0.nx, p0.ny, p0.nz, npk * G, st, 1, 2, 0, &sc.blue, ft.form));
+  {
+    const int slot = ctx.prof.begin(kDc, st);
+    k_dc<<<1, (npk * G + 31) / 32 * 32, 0, st>>>(spec, npk * G, nvox, p0.nx, p0.ny, p0.nz, 0, 1 % p0.nz, p0.nz - 1,
+                                                 sc.dc.as<float2>());
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+  }
+  // Ewald projection, rotation and detector warp over the virtual energies
+  FieldEwaldParams fe{};
+  fe.zspec = spec;
+  fe.zdc = sc.dc.as<float2>();
+  fe.npk = npk;
+  fe.nvox = nvox;
+  fe.coef = reinterpret_cast<const float4 *>(dp + off_c);
+  fe.kmag = reinterpret_cast<const float *>(dp + off_k);
+  fe.e_per_req = E;
+  fe.g.start = -static_cast<float>(kPi / o->phys_size);
+  fe.g.dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((p0.nx - 1) * 1.0));
+  fe.g.dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((p0.ny - 1) * 1.0));
+  fe.g.dz = p0.twod ? 0.f : static_cast<float>((2.0 * kPi / o->phys_size) / ((p0.nz - 1) * 1.0));
+  fe.g.nx = p0.nx, fe.g.ny = p0.ny, fe.g.nz = p0.nz;
+  fe.g.interp = o->ewald_interpolation;
+  fe.g.twod = p0.twod ? 1u : 0u;
+  fe.qx = reinterpret_cast<const float *>(dp + p0.off_qx);
+  fe.qy = reinterpret_cast<const float *>(dp + p0.off_qy);
+  fe.qz = reinterpret_cast<const float *>(dp + p0.off_qz);
+  fe.nangles = p0.nang;
+  fe.images = sc.images.as<float>();
+  fe.gram = sc.images.as<float4>();
+  fe.gplane = gram_plane_size(int(p0.ny), int(p0.nx));
+  const KFrame &f = p0.frames[0];
+  fe.kvx = f.k.x, fe.kvy = f.k.y, fe.kvz = f.k.z;
+  fe.mat = reinterpret_cast<const float *>(dp + p0.off_mat);
+  fe.ecoef = reinterpret_cast<const float *>(dp + p0.off_coef);
+  RotateGramParams rg{};
+  rg.gram = sc.images.as<float4>();
+  rg.plane = fe.gplane;
+  rg.coef = reinterpret_cast<const WarpCoef *>(dp + p0.off_warp);
+  rg.ecoef = fe.ecoef;
+  rg.W = W, rg.H = H;
+  rg.nangles = p0.nang;
+  rg.rot_mask = o->rot_mask;
+  rg.avg = sc.avg.as<float>();
+  const size_t fsmem = size_t(kEwaldEnergies) * 6 * npk * sizeof(float4);
+  const unsigned fpix_blocks = unsigned((npix + 31) / 32), pix_blocks = unsigned((npix + 255) / 256);
+  const unsigned rot_tiles = unsigned(((W + kRotTile - 1) / kRotTile) * ((H + kRotTile - 1) / kRotTile));
+  const size_t rsm = p0.has_rows ? size_t(H) * sizeof(int2) : 0;
+  const float fillv = o->rot_mask ? 0.f : std::numeric_limits<float>::quiet_NaN();
+  float *const *out_g = reinterpret_cast<float *const *>(dp + off_o);
+  for (uint32_t e0 = 0; e0 < total; e0 += vb) {
+    const uint32_t nb = std::min(vb, total - e0);
+    fe.e0 = e0;
+    fe.nbatch = nb;
+    rg.nenergies = nb;
+    rg.rows = p0.has_rows ? reinterpret_cast<const int2 *>(dp + off_r) + size_t(e0) * H : nullptr;
+    int slot = ctx.prof.begin(kEwaldFields, st);
+    k_ewald_fields<2><<<fpix_blocks * ((nb + kEwaldEnergies - 1) / kEwaldEnergies), kFieldEwaldThreads, fsmem, st>>>(fe);
+    ctx.prof.end(slot, st);
+    slot = ctx.prof.begin(kRotateGram, st);
+    k_rotate_gram<2, packed_energies<2>()><<<dim3(rot_tiles, (nb + nep - 1) / nep), kRotTile * kRotTile, rsm, st>>>(rg);
+    ctx.prof.end(slot, st);
+    slot = ctx.prof.begin(kWarp, st);
+    k_warp_group<<<dim3(pix_blocks, nb), 256, 0, st>>>(sc.avg.as<float>(), out_g, E, e0, W, H, p0.detector_warp[0],
+                                                       fillv);
+    ctx.prof.end(slot, st);
+    CYR_CUDA(cudaGetLastError());
+  }
+  CYR_CUDA(cudaEventRecord(sc.last_use, st));
   return CYR_OK;
 }
 
@@ -2283,17 +2530,7 @@ int start_request(Server &S, Slot &sl, ServerRequest &r) {
     d_out = sl.out.as<float>();
   }
   const Plan &pl = r.plan;
-  if (pl.arena.size() > sl.host_arena_bytes) {
-    if (sl.host_arena) {
-      CYR_CUDA(cudaStreamSynchronize(st));
-      cudaFreeHost(sl.host_arena);
-      sl.host_arena = nullptr;
-    }
-    for (auto &kv : sl.graphs) cudaGraphExecDestroy(kv.second.exec);  // their upload nodes read the old copy
-    sl.graphs.clear();
-    sl.host_arena_bytes = std::max<size_t>(pl.arena.size(), 64 * 1024);
-    CYR_CUDA(cudaMallocHost(&sl.host_arena, sl.host_arena_bytes));
-  }
+  CYR_TRY(ensure_host_arena(sl, pl.arena.size()));  // graphs' upload nodes read the old copy: dropped on growth
   RunMode mode;
   mode.host_arena = sl.host_arena;
   mode.host_arena_bytes = sl.host_arena_bytes;
@@ -2342,19 +2579,34 @@ int start_request(Server &S, Slot &sl, ServerRequest &r) {
   return CYR_OK;
 }
 
+// Enqueues a group of same-key requests on slot sl (worker thread).
+int start_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerRequest>> &g) {
+  CYR_TRY(run_group(S, sl, g));
+  CYR_CUDA(cudaMemcpyAsync(sl.host_errors, sl.sc.errors.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, sl.stream));
+  CYR_CUDA(cudaEventRecord(sl.done, sl.stream));
+  ++S.group_runs;
+  S.grouped += g.size();
+  return CYR_OK;
+}
+
 void finish_request(Server &S, Slot &sl, int status, const std::string &err) {
-  std::shared_ptr<ServerRequest> r = sl.req;
+  std::vector<std::shared_ptr<ServerRequest>> rs{sl.req};
+  rs.insert(rs.end(), sl.group.begin(), sl.group.end());
   sl.req.reset();
+  sl.group.clear();
   std::lock_guard<std::mutex> lk(S.mu);
-  r->t_done = Clock::now();
-  r->status = status;
-  r->error = err;
-  S.in_use -= std::min(S.in_use, r->footprint);
-  S.inflight_work = std::max(0.0, S.inflight_work - r->work);
-  if (status == CYR_OK)
-    ++S.completed;
-  else
-    ++S.failed;
+  const Clock::time_point now = Clock::now();
+  for (const auto &r : rs) {
+    r->t_done = now;
+    r->status = status;
+    r->error = err;
+    S.in_use -= std::min(S.in_use, r->footprint);
+    S.inflight_work = std::max(0.0, S.inflight_work - r->work);
+    if (status == CYR_OK)
+      ++S.completed;
+    else
+      ++S.failed;
+  }
   S.cv_done.notify_all();
 }
 
@@ -2406,6 +2658,7 @@ void server_loop(Server *Sp) {
                                                                                     : 0;
         if (score > best) best = score, free_slot = &sl;
       }
+      std::vector<std::shared_ptr<ServerRequest>> grp;  // requests sharing r's launches
       {
         std::lock_guard<std::mutex> lk(S.mu);
         if (!free_slot) break;
@@ -2414,11 +2667,35 @@ void server_loop(Server *Sp) {
         S.queue.pop_front();
         S.in_use += r->footprint;
         S.inflight_work += r->work;
-        r->t_start = Clock::now();
+        const Clock::time_point now = Clock::now();
+        r->t_start = now;
+        if (S.groups && !r->group_key.empty()) {
+          // queued requests of the same key join r, as far as the budget allows
+          const uint32_t cap = std::min<uint32_t>(kMaxGroup, std::max<uint32_t>(1, 1024 / r->plan.npk));
+          for (auto it = S.queue.begin(); it != S.queue.end() && grp.size() + 1 < cap;) {
+            if ((*it)->group_key == r->group_key && S.in_use + (*it)->footprint <= S.budget) {
+              S.in_use += (*it)->footprint;
+              S.inflight_work += (*it)->work;
+              (*it)->t_start = now;
+              grp.push_back(*it);
+              it = S.queue.erase(it);
+            } else {
+              ++it;
+            }
+          }
+        }
       }
       progress = true;
       free_slot->req = r;
-      const int rc = start_request(S, *free_slot, *r);
+      free_slot->group = grp;
+      int rc;
+      if (grp.empty()) {
+        rc = start_request(S, *free_slot, *r);
+      } else {
+        std::vector<std::shared_ptr<ServerRequest>> all{r};
+        all.insert(all.end(), grp.begin(), grp.end());
+        rc = start_group(S, *free_slot, all);
+      }
       if (rc != CYR_OK) {
         const std::string err = g_error;
         cudaStreamSynchronize(free_slot->stream);  // let whatever was enqueued finish before the slot is reused
@@ -2948,6 +3225,7 @@ int cyr_server_create(uint32_t slots, size_t hbm_budget, uint32_t flags, cyr_ser
   S->ctx = ctx;
   S->device = ctx->device;
   S->graphs = (flags & CYR_SERVER_GRAPHS) != 0;
+  S->groups = (flags & CYR_SERVER_GROUPS) != 0;
   if (hbm_budget == 0) {
     size_t free_b = 0, total_b = 0;
     CYR_CUDA(cudaMemGetInfo(&free_b, &total_b));
@@ -3042,6 +3320,14 @@ int cyr_server_stats(cyr_server *s, uint64_t *completed, uint64_t *failed, uint6
   if (failed) *failed = S.failed;
   if (graph_replays) *graph_replays = S.replays;
   if (graph_captures) *graph_captures = S.captures;
+  return CYR_OK;
+}
+
+int cyr_server_group_stats(cyr_server *s, uint64_t *group_runs, uint64_t *grouped_requests) {
+  if (!s) return fail(CYR_ERR_ARGUMENT, "null server");
+  Server &S = *s->impl;
+  if (group_runs) *group_runs = S.group_runs;
+  if (grouped_requests) *grouped_requests = S.grouped;
   return CYR_OK;
 }
 

@@ -59,6 +59,10 @@ __device__ __forceinline__ void field_means(const double *__restrict__ mom, uint
 
 struct FieldParams {
   const float4 *vox;     // [nmat][nvox] as the reference stores Voxel::s1
+  // request group (blockIdx.y = request): its morphologies, and the strides of
+  // its moments and packed volumes; null for a single request
+  const float4 *const *vox_g;
+  size_t mom_stride, out_stride;
   uint32_t nx, ny, nz, nmat;
   size_t nvox;
   const double *mom;     // [nmat][kMoments] moment sums over nsamp voxels
@@ -69,9 +73,18 @@ struct FieldParams {
 };
 
 // Windowed, mean-free fields of every voxel, packed in pairs.
+// Selects request blockIdx.y of a request group.
+__device__ __forceinline__ void field_group(FieldParams &p) {
+  if (!p.vox_g) return;
+  p.vox = p.vox_g[blockIdx.y];
+  p.mom += size_t(blockIdx.y) * p.mom_stride;
+  p.out += size_t(blockIdx.y) * p.out_stride;
+}
+
 template <int MORPH>
 __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
   __shared__ float mean[kMaxFields];  // volume mean of each windowed field
+  field_group(p);
   field_means(p.mom, p.nmat, p.nsamp, mean);
   __syncthreads();
   const size_t stride = size_t(gridDim.x) * blockDim.x;
@@ -136,6 +149,7 @@ __global__ void __launch_bounds__(256, V <= 16 ? 3 : 1) k_build_fields_rows(Fiel
   float2 *tws = fsm;        // the warp FFT's stage twiddles (N - radix entries)
   float2 *lines = fsm + N;  // [npk][N]: element x of line j at lines[j N + swz(x)]
   __shared__ float mean[kMaxFields];
+  field_group(p);
   field_means(p.mom, p.nmat, p.nsamp, mean);
   warp_twiddles<V>(tws, tw_n);
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -229,6 +243,9 @@ struct FieldEwaldParams {
   float4 *gram;          // NB > 0: Gram records [batch / NEP][RQ][gplane] (GramRec<NB, packed_energies<NB>()>, gram_at)
   size_t gplane;         // float4 per Gram plane (gram_plane_size(ny, nx))
   uint32_t nbatch;       // energies of this launch
+  // request group: energy e belongs to request e / e_per_req, whose packed volumes start at
+  // zspec + request * npk * nvox (DC at zdc + request * npk); 0 for a single request
+  uint32_t e_per_req;
 };
 
 constexpr int kEwaldEnergies = 4;  // energies (warps) per block
@@ -261,6 +278,11 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   const size_t t = size_t(blockIdx.x / ngrp) * 32 + (threadIdx.x & 31);
   if (t >= npix) return;
   const uint32_t Y = uint32_t(t / nx), X = uint32_t(t % nx);
+  if (p.e_per_req) {
+    const uint32_t rq = e / p.e_per_req;
+    p.zspec += size_t(rq) * p.npk * p.nvox;
+    p.zdc += size_t(rq) * p.npk;
+  }
   EwaldGeom g = p.g;
   g.kmag = p.kmag[e];
   g.kx = __fmul_rn(g.kmag, p.kvx), g.ky = __fmul_rn(g.kmag, p.kvy), g.kz = __fmul_rn(g.kmag, p.kvz);

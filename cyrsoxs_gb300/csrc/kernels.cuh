@@ -142,6 +142,7 @@ __device__ __forceinline__ void nt_entries(const BuildParams &p, const MaterialC
 constexpr int kMoments = 7;
 struct MomentParams {
   const float4 *vox;
+  const float4 *const *vox_g;  // request group (blockIdx.z = request): its morphologies, or null
   uint32_t nx, ny, nz, nmat;
   size_t nvox;
   const float *hann_x, *hann_y, *hann_z;
@@ -155,6 +156,10 @@ template <int MORPH>
 __global__ void __launch_bounds__(256) k_moments(MomentParams p) {
   __shared__ double red[8][kMoments];
   const uint32_t m = blockIdx.y;
+  if (p.vox_g) {  // a request group: request blockIdx.z's morphology and moments
+    p.vox = p.vox_g[blockIdx.z];
+    p.out += size_t(blockIdx.z) * p.nmat * kMoments;
+  }
   // per-thread sums in float (a few hundred terms; only an approximate mean is
   // needed), block and grid reduction in double
   float acc[kMoments];
@@ -2041,6 +2046,20 @@ __global__ void __launch_bounds__(kRotTile * kRotTile, 3) k_rotate_gram(RotateGr
 #pragma unroll
   for (int s = 0; s < NEP; ++s)
     if (s < ne) p.avg[(size_t(group) * NEP + s) * npix + size_t(yd) * p.W + xd] = angle_mean(sum[s], count[s], p.nangles, p.rot_mask);
+}
+
+// Detector warp of a request group's angle averages (one image per virtual
+// energy ve = ve0 + blockIdx.y, request ve / e_per_req): the fill and the warp of
+// k_fill + k_warp in one pass, written to that request's own projection.
+__global__ void k_warp_group(const float *__restrict__ src, float *const *__restrict__ out_g, uint32_t e_per_req,
+                             uint32_t ve0, int W, int H, WarpCoef c, float prefill) {
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const size_t npix = size_t(W) * H;
+  if (t >= npix) return;
+  const uint32_t ve = ve0 + blockIdx.y;  // src holds the launch's images from ve0 on
+  float v;
+  if (!warp_sample(src + size_t(blockIdx.y) * npix, W, H, c, int(t % W), int(t / W), v)) v = prefill;
+  out_g[ve / e_per_req][size_t(ve % e_per_req) * npix + t] = v;
 }
 
 __global__ void k_fill(float *dst, size_t n, float v, size_t stride = 0) {

@@ -1,6 +1,6 @@
 """Serving engine (continuous batching) over the C ABI: cyr_server_*.
 
-    srv = Server(slots=8, graphs=True)
+    srv = Server(slots=8, graphs=True, groups=True)
     rid = srv.submit(opts, optical, voxels, out)          # host arrays (keep them alive)
     rid = srv.submit(opts, optical, d_vox_ptr, d_out_ptr, device=True)
     latency_s, queue_s = srv.wait(rid)
@@ -19,6 +19,7 @@ import numpy as np
 from . import _native
 
 GRAPHS = 1
+GROUPS = 2
 
 
 def _bind(L):
@@ -32,6 +33,7 @@ def _bind(L):
     L.cyr_server_wait.argtypes = [vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(ctypes.c_double)]
     L.cyr_server_stats.argtypes = [vp] + [ctypes.POINTER(ctypes.c_uint64)] * 4
+    L.cyr_server_group_stats.argtypes = [vp] + [ctypes.POINTER(ctypes.c_uint64)] * 2
     L.cyr_server_destroy.argtypes = [vp]
     L._serving_bound = True
     return L
@@ -40,11 +42,11 @@ def _bind(L):
 class Server:
     """A serving engine on the current CUDA device."""
 
-    def __init__(self, slots: int = 8, hbm_budget: int = 0, graphs: bool = False):
+    def __init__(self, slots: int = 8, hbm_budget: int = 0, graphs: bool = False, groups: bool = False):
         self._L = _bind(_native.lib())
         h = ctypes.c_void_p()
-        _native.check(self._L.cyr_server_create(int(slots), int(hbm_budget), GRAPHS if graphs else 0,
-                                                ctypes.byref(h)))
+        flags = (GRAPHS if graphs else 0) | (GROUPS if groups else 0)
+        _native.check(self._L.cyr_server_create(int(slots), int(hbm_budget), flags, ctypes.byref(h)))
         self._h = h
         self._keep = {}  # id -> objects the request reads or writes until it is done
 
@@ -82,7 +84,10 @@ class Server:
     def stats(self) -> dict:
         v = [ctypes.c_uint64() for _ in range(4)]
         _native.check(self._L.cyr_server_stats(self._h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("completed", "failed", "graph_replays", "graph_captures"), (x.value for x in v)))
+        g = [ctypes.c_uint64() for _ in range(2)]
+        _native.check(self._L.cyr_server_group_stats(self._h, *[ctypes.byref(x) for x in g]))
+        return dict(zip(("completed", "failed", "graph_replays", "graph_captures", "group_runs", "grouped_requests"),
+                        (x.value for x in v + g)))
 
     def close(self):
         if self._h:

@@ -261,6 +261,14 @@ CYR_API uint32_t cyr_num_stages(void);
  * ------------------------------------------------------------------------ */
 typedef struct cyr_server cyr_server;
 #define CYR_SERVER_GRAPHS 1u
+/* With CYR_SERVER_GROUPS, queued requests that differ only in morphology,
+ * energies and optical constants (FIELDS strategy, LAB frame, k along z,
+ * device buffers, same shape, angles and options) are admitted together, up
+ * to 16 at a time, and share one launch per kernel: the transform runs over
+ * all their packed volumes at once, and the Ewald projection, rotation and
+ * detector warp over all their energies.  Each request still computes
+ * exactly what it computes alone. */
+#define CYR_SERVER_GROUPS 2u
 
 CYR_API int cyr_server_create(uint32_t slots, size_t hbm_budget, uint32_t flags, cyr_server **server);
 
@@ -282,6 +290,9 @@ CYR_API int cyr_server_wait(cyr_server *server, uint64_t id, double *latency_s, 
 
 CYR_API int cyr_server_stats(cyr_server *server, uint64_t *completed, uint64_t *failed, uint64_t *graph_replays,
                              uint64_t *graph_captures);
+
+/* Number of grouped launches (CYR_SERVER_GROUPS) and the requests they served. */
+CYR_API int cyr_server_group_stats(cyr_server *server, uint64_t *group_runs, uint64_t *grouped_requests);
 
 /* Finishes the queued requests, then frees the slots. */
 CYR_API int cyr_server_destroy(cyr_server *server);

@@ -147,3 +147,55 @@ def test_one_slot_alternating_signatures_after_a_capture():
         st = srv.stats()
     # B's first run may grow the slot's buffers, which retires A's graph (it is captured again later)
     assert st["failed"] == 0 and st["graph_captures"] >= 2 and st["graph_replays"] >= 1
+
+
+# Request groups (CYR_SERVER_GROUPS): same-shape FIELDS requests on device buffers, queued behind a
+# running request, share one launch per kernel; each must equal its own cuda_main result.
+GROUP_SHAPES = [
+    # (nx, nz, materials, energies, windowing, rot_mask): warp-FFT rows (fused build) and 40-point rows
+    (64, 16, 2, [281.0, 284.0, 285.5, 289.0], 0, 0),
+    (128, 32, 3, [283.0, 286.0, 287.0], 1, 1),
+    (40, 8, 2, [284.0, 286.0], 0, 0),
+]
+
+
+@pytest.mark.parametrize("shape", GROUP_SHAPES, ids=lambda s: f"{s[0]}x{s[0]}x{s[1]}m{s[2]}")
+def test_grouped_requests_equal_their_single_results(shape):
+    torch, nat, serving = _setup()
+    nx, nz, m, es, win, mask = shape
+    members = []
+    for i in range(6):
+        c = cases.Case(f"grp{i}", nx, nx, nz, m, [e + 0.5 * i for e in es], seed=90 + i, geometry="blobs",
+                       windowing=win, rot_mask=mask, angles=(0.0, 150.0, 30.0))
+        o = options_for(nat, c, strategy=2)
+        opt, v = cases.optical_constants(c), np.ascontiguousarray(cases.voxels(c), np.float32)
+        members.append((o, opt, torch.from_numpy(v).cuda(), nat.cuda_main(o, opt, v), c))
+    outs = [torch.zeros(w.size, dtype=torch.float32, device="cuda") for _, _, _, w, _ in members]
+    torch.cuda.synchronize()
+    with serving.Server(slots=1, groups=True) as srv:
+        # the first request occupies the only slot, so the other five queue and are admitted as one group
+        ids = [srv.submit(o, opt, dv.data_ptr(), out.data_ptr(), device=True)
+               for (o, opt, dv, _, _), out in zip(members, outs)]
+        for rid in ids:
+            srv.wait(rid)
+        st = srv.stats()
+    assert st["group_runs"] >= 1 and st["grouped_requests"] >= 2, st
+    for (o, opt, dv, want, c), out in zip(members, outs):
+        same(out.cpu().numpy().reshape(want.shape), want)
+
+
+def test_groups_and_graphs_mix_with_other_requests():
+    torch, nat, serving = _setup()
+    reqs = mix_requests(nat)
+    alone = {n: nat.cuda_main(o, opt, v, streams_variant=c.algorithm == 1) for n, o, opt, v, c in reqs}
+    dev = {n: torch.from_numpy(v).cuda() for n, o, opt, v, c in reqs}
+    with serving.Server(slots=2, graphs=True, groups=True) as srv:
+        for rnd in range(2):
+            outs, ids = {}, {}
+            for n, o, opt, v, c in reqs + reqs:  # each request twice: same-key pairs can group
+                key = (n, len(ids))
+                outs[key] = torch.zeros(alone[n].size, dtype=torch.float32, device="cuda")
+                ids[key] = srv.submit(o, opt, dev[n].data_ptr(), outs[key].data_ptr(), device=True)
+            for key, rid in ids.items():
+                srv.wait(rid)
+                same(outs[key].cpu().numpy().reshape(alone[key[0]].shape), alone[key[0]])
