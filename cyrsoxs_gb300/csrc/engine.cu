@@ -118,10 +118,15 @@ bool smooth7(uint32_t n) {
   return factorize(n, r);
 }
 
-// Lengths with a prime factor above 7 run as Bluestein transforms over the
-// smallest 7-smooth M >= 2N - 1, itself limited to one block's FFT.
+// Lengths with a prime factor above 7 run as Bluestein transforms over a
+// padded length M >= 2N - 1, itself limited to one block's FFT: the next power
+// of two while that is at most 1024 (the warp FFT's lengths), else the
+// smallest 7-smooth M.
 constexpr uint32_t kMaxBluesteinPad = 4096;
 uint32_t bluestein_length(uint32_t n) {
+  uint32_t p2 = 128;
+  while (p2 < 2 * n - 1) p2 *= 2;
+  if (p2 <= 1024) return p2;
   uint32_t m = 2 * n - 1;
   while (!smooth7(m)) ++m;
   return m;
@@ -1308,7 +1313,7 @@ int build_fields_x(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const 
   CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
   fp.i0 = size_t(z0) * pl.npix, fp.i1 = size_t(z1) * pl.npix;
   if (fused) {
-    const size_t smem = fields_rows_smem(pl.nx, npk);
+    const size_t smem = fields_rows_smem(pl.nx, npk, pl.nmat);
     const uint32_t rows = (z1 - z0) * pl.ny;
     int per_sm = 1;
     auto launch = [&](auto kern) -> int {
@@ -1424,7 +1429,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   fp.out = spec;
   // the field build fused with the x pass when x is a warp-FFT length and the row's lines fit
   const bool fused_ok = (pl.nx == 128 || pl.nx == 256 || pl.nx == 512 || pl.nx == 1024) &&
-                        fields_rows_smem(pl.nx, npk) <= kFftSmemBudget;
+                        fields_rows_smem(pl.nx, npk, pl.nmat) <= kFftSmemBudget;
   const float2 *twx = nullptr;
   if (fused_ok) CYR_TRY(get_twiddles(ctx, pl.nx, &twx));
   // tuned launch forms of this shape, tuned here on its first device-resident request
@@ -2397,7 +2402,7 @@ int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerReque
   fp.i0 = 0, fp.i1 = nvox;
   if (p0.hanning) fp.hann_x = mp.hann_x, fp.hann_y = mp.hann_y, fp.hann_z = mp.hann_z;
   const bool fused_ok = (p0.nx == 128 || p0.nx == 256 || p0.nx == 512 || p0.nx == 1024) &&
-                        fields_rows_smem(p0.nx, npk) <= kFftSmemBudget;
+                        fields_rows_smem(p0.nx, npk, nmat) <= kFftSmemBudget;
   DeviceContext::FieldTune ft;
   {
     char key[96];
@@ -2409,7 +2414,7 @@ int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerReque
   if (fused_ok && ft.fused) {
     const float2 *twx = nullptr;
     CYR_TRY(get_twiddles(ctx, p0.nx, &twx));
-    const size_t smem = fields_rows_smem(p0.nx, npk);
+    const size_t smem = fields_rows_smem(p0.nx, npk, nmat);
     const uint32_t rws = p0.nz * p0.ny;
     int per_sm = 1;
     auto launch = [&](auto kern) -> int {
