@@ -656,7 +656,8 @@ int bluestein_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, u
   CYR_TRY(get_blue(ctx, n, bt));
   const uint32_t lpv = axis == 0 ? ny * nz : axis == 1 ? nx * nz : nx * ny;
   const uint64_t total = uint64_t(lpv) * count;
-  const uint64_t cap = std::max<uint64_t>(1, (size_t(256) << 20) / (size_t(bt.m) * sizeof(float2)));
+  // a multiple of 32 lines per chunk, so the column pass of y and z lines can use TMA tiles
+  const uint64_t cap = std::max<uint64_t>(32, (size_t(256) << 20) / (size_t(bt.m) * sizeof(float2)) / 32 * 32);
   const uint32_t chunk = uint32_t(std::min<uint64_t>(total, cap));
   CYR_TRY(work->ensure(size_t(chunk) * bt.m * sizeof(float2)));
   int sms = 0;
@@ -681,12 +682,20 @@ int bluestein_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, u
     if (axis == 2) k_blue_gather<2><<<grid, 256, 0, st>>>(p);
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
-    CYR_TRY(fft_axes(ctx, p.work, bt.m, p.nlines, 1, 1, st, 0, 0));  // m is 7-smooth
+    // m is 7-smooth: rows of m (x lines) or columns of m (y and z lines)
+    auto padded_fft = [&]() -> int {
+      if (axis == 0) return fft_axes(ctx, p.work, bt.m, p.nlines, 1, 1, st, 0, 0);
+      return fft_axes(ctx, p.work, p.nlines, bt.m, 1, 1, st, 1, 1);
+    };
+    CYR_TRY(padded_fft());
     slot = ctx.prof.begin(kBluestein, st);
-    k_blue_mul<<<grid, 256, 0, st>>>(p);
+    if (axis == 0)
+      k_blue_mul<0><<<grid, 256, 0, st>>>(p);
+    else
+      k_blue_mul<1><<<grid, 256, 0, st>>>(p);
     ctx.prof.end(slot, st);
     CYR_CUDA(cudaGetLastError());
-    CYR_TRY(fft_axes(ctx, p.work, bt.m, p.nlines, 1, 1, st, 0, 0));
+    CYR_TRY(padded_fft());
     slot = ctx.prof.begin(kBluestein, st);
     if (axis == 0) k_blue_scatter<0><<<grid, 256, 0, st>>>(p);
     if (axis == 1) k_blue_scatter<1><<<grid, 256, 0, st>>>(p);

@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
       for (int u = 0; u < 4; ++u) {
         if (m0 + u >= p.nmat) break;
         float sx, sy, sz, pa, pui;
-        director_fields<MORPH>(sv[u], sx, sy, sz, pa, pui);
+        director<MORPH>(sv[u], sx, sy, sz, pa, pui);
         const float wa = w * pa;
         const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
         T += f0 + f1 + f2 + f6;
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(256, V <= 16 ? 2 : 1) k_build_fields_rows(Fiel
       };
       for (uint32_t m = 0; m < p.nmat; ++m) {
         float sx, sy, sz, pa, pui;
-        director_fields<MORPH>(stage[m * N + x], sx, sy, sz, pa, pui);
+        director<MORPH>(stage[m * N + x], sx, sy, sz, pa, pui);
         const float wa = w * pa;
         const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
         T += f0 + f1 + f2 + f6;

@@ -68,41 +68,6 @@ struct BuildParams {
 };
 
 // Direction and fractions of one material at one voxel.
-// sin and cos of an angle for the field build: the angle is brought to
-// [-pi, pi] with 2 pi split into two floats (Cody-Waite), then the hardware
-// approximation is used (absolute error below 1e-6 there); angles beyond
-// +-25 rad keep the accurate library routine.
-__device__ __forceinline__ void sincos_reduced(float x, float *sn, float *cs) {
-  if (fabsf(x) <= 25.f) {
-    const float k = rintf(x * 0.159154943091895336f);  // x / (2 pi)
-    float r = fmaf(-k, 6.28318548202514648f, x);      // 2 pi rounded to float
-    r = fmaf(-k, -1.74845553146951715e-7f, r);         // minus the rounding of 2 pi
-    __sincosf(r, sn, cs);
-  } else {
-    sincosf(x, sn, cs);
-  }
-}
-
-// The director of the FIELDS build (k_build_fields, k_build_fields_rows): the
-// same as director<MORPH> with sincos_reduced for the Euler angles.
-template <int MORPH>
-__device__ __forceinline__ void director_fields(float4 s, float &sx, float &sy, float &sz, float &pa, float &pui) {
-  if (MORPH == 0) {
-    float st, ct, sp, cp;
-    sincos_reduced(s.y, &st, &ct);
-    sincos_reduced(s.z, &sp, &cp);
-    sx = cp * st;
-    sy = sp * st;
-    sz = ct;
-    pa = s.w * s.x;
-    pui = s.w - pa;
-  } else {
-    sx = s.x, sy = s.y, sz = s.z;
-    pa = 1.f;
-    pui = s.w;
-  }
-}
-
 template <int MORPH>
 __device__ __forceinline__ void director(float4 s, float &sx, float &sy, float &sz, float &pa, float &pui) {
   if (MORPH == 0) {  // Euler: s1 = (S, theta, psi, Vfrac), uniaxial.h:82-92
@@ -600,12 +565,13 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
 // inverse transform is conj(FFT(conj(y))) / M.  Chirp and table are formed in
 // double on the host (j^2 reduced mod 2N in integers) and rounded to float.
 // The lines of a pass are processed in chunks of `nlines` padded lines held
-// in `work` [nlines][M]; consecutive threads take consecutive x for y and z
-// lines, so the strided gathers and scatters stay coalesced.
+// in `work`: [nlines][M] for x lines (the padded FFT is a row pass), [M][nlines]
+// for y and z lines (a column pass), so every gather, product and scatter
+// reads and writes contiguous memory.
 // ---------------------------------------------------------------------------
 struct BlueParams {
   float2 *data;           // the volumes being transformed
-  float2 *work;           // [nlines][m]
+  float2 *work;           // x lines: [nlines][m]; y and z lines: [m][nlines] (lines fastest)
   const float2 *chirp;    // c_j, j < n
   const float2 *bhat;     // FFT_m(b) / m
   uint32_t nx, ny, nz;    // volume dimensions (nz: the planes this call covers)
@@ -635,7 +601,9 @@ __device__ __forceinline__ size_t blue_line(const BlueParams &p, uint64_t line, 
   return base;
 }
 
-// work[l][j] = x_j c_j (j < n), 0 (n <= j < m)
+// work = x_j c_j (j < n), 0 (n <= j < m).  Thread t takes element t of the
+// work buffer, so its stores are contiguous; for y and z lines consecutive
+// lines are consecutive x, so the volume reads are contiguous too.
 template <int AXIS>
 __global__ void k_blue_gather(BlueParams p) {
   const size_t total = size_t(p.nlines) * p.m;
@@ -652,31 +620,35 @@ __global__ void k_blue_gather(BlueParams p) {
       const size_t b = blue_line<AXIS>(p, p.line0 + l, es);
       v = cmul(p.data[b + j * es], p.chirp[j]);
     }
-    p.work[size_t(l) * p.m + j] = v;
+    p.work[t] = v;
   }
 }
 
 // work = conj(work * bhat): the product of the transforms, conjugated for the inverse
+template <int AXIS>
 __global__ void k_blue_mul(BlueParams p) {
   const size_t total = size_t(p.nlines) * p.m;
   for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
-    const float2 w = cmul(p.work[t], p.bhat[t % p.m]);
+    const float2 w = cmul(p.work[t], p.bhat[AXIS == 0 ? t % p.m : t / p.nlines]);
     p.work[t] = make_float2(w.x, -w.y);
   }
 }
 
-// x_k = c_k conj(work[l][k]), k < n
+// x_k = c_k conj(work element k of line l), k < n
 template <int AXIS>
 __global__ void k_blue_scatter(BlueParams p) {
   const size_t total = size_t(p.nlines) * p.n;
   for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
     uint32_t l, k;
+    size_t wi;
     if (AXIS == 0) {
       l = uint32_t(t / p.n), k = uint32_t(t % p.n);
+      wi = size_t(l) * p.m + k;
     } else {
       l = uint32_t(t % p.nlines), k = uint32_t(t / p.nlines);
+      wi = t;  // element k of line l at k nlines + l
     }
-    const float2 w = p.work[size_t(l) * p.m + k];
+    const float2 w = p.work[wi];
     size_t es;
     const size_t b = blue_line<AXIS>(p, p.line0 + l, es);
     p.data[b + k * es] = cmul(p.chirp[k], make_float2(w.x, -w.y));
