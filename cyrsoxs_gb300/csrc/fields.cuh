@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
       for (int u = 0; u < 4; ++u) {
         if (m0 + u >= p.nmat) break;
         float sx, sy, sz, pa, pui;
-        director<MORPH>(sv[u], sx, sy, sz, pa, pui);
+        director_fields<MORPH>(sv[u], sx, sy, sz, pa, pui);
         const float wa = w * pa;
         const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
         T += f0 + f1 + f2 + f6;
@@ -140,44 +140,33 @@ __global__ void __launch_bounds__(256) k_build_fields(FieldParams p) {
 // FFT with that line as its exchange buffer, and stores the transformed row.
 // The packed volumes leave the chip once, already x-transformed: the build's
 // write and the row pass's read-back of 8 npk bytes per voxel are gone.
-// The morphology of the block's next row is copied into shared memory with
-// cp.async while the current row is transformed, so the build phase reads
-// its voxels from shared memory.  Shared memory: (npk + 1) N float2 (lines and
-// twiddles) and nmat N float4 (the staged voxels).
+// Shared memory: (npk + 1) N float2 (lines and twiddles).  Three blocks per SM
+// (80 registers) measured faster than two blocks that also stage the next
+// row's voxels in shared memory with cp.async.
 __host__ __device__ constexpr size_t fields_rows_smem(uint32_t n, uint32_t npk, uint32_t nmat) {
-  return size_t(npk + 1) * n * sizeof(float2) + size_t(nmat) * n * sizeof(float4);
+  return (void)nmat, size_t(npk + 1) * n * sizeof(float2);
 }
 
 template <int MORPH, int V>
-__global__ void __launch_bounds__(256, V <= 16 ? 2 : 1) k_build_fields_rows(FieldParams p, const float2 *__restrict__ tw_n,
+__global__ void __launch_bounds__(256, V <= 16 ? 3 : 1) k_build_fields_rows(FieldParams p, const float2 *__restrict__ tw_n,
                                                                             uint32_t npk) {
   constexpr uint32_t N = 32 * V;
-  extern __shared__ float4 fsm4[];
-  float4 *stage = fsm4;                                                         // [nmat][N] voxels of the next row
-  float2 *tws = reinterpret_cast<float2 *>(fsm4 + size_t(p.nmat) * N);          // warp FFT stage twiddles
-  float2 *lines = tws + N;  // [npk][N]: element x of line j at lines[j N + swz(x)]
+  extern __shared__ float2 fsm[];
+  float2 *tws = fsm;        // the warp FFT's stage twiddles (N - radix entries)
+  float2 *lines = fsm + N;  // [npk][N]: element x of line j at lines[j N + swz(x)]
   __shared__ float mean[kMaxFields];
   field_group(p);
   field_means(p.mom, p.nmat, p.nsamp, mean);
   warp_twiddles<V>(tws, tw_n);
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const uint32_t nrows = uint32_t((p.i1 - p.i0) / N);
-  auto prefetch = [&](uint32_t r) {
-    const size_t rowbase = p.i0 + size_t(r) * N;
-    for (uint32_t t = threadIdx.x; t < p.nmat * N; t += blockDim.x) {
-      const uint32_t m = t / N, x = t % N;
-      cp_async16(&stage[t], &p.vox[size_t(m) * p.nvox + rowbase + x]);
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-  };
-  if (blockIdx.x < nrows) prefetch(blockIdx.x);
   for (uint32_t r = blockIdx.x; r < nrows; r += gridDim.x) {
-    cp_async_wait_all();
-    __syncthreads();  // staged voxels landed; means and twiddles ready; the previous row's lines consumed
+    __syncthreads();  // means and twiddles ready; the previous row's lines consumed
     const size_t rowbase = p.i0 + size_t(r) * N;
     const uint32_t y = uint32_t((rowbase / N) % p.ny), z = uint32_t(rowbase / (size_t(N) * p.ny));
     const float wyz = p.hann_x ? p.hann_y[y] * p.hann_z[z] : 1.f;
     for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+      const size_t i = rowbase + x;
       const float w = p.hann_x ? p.hann_x[x] * wyz : 1.f;
       float2 *o = lines + swz(x);
       float T = 0.f, pend = 0.f;
@@ -190,25 +179,32 @@ __global__ void __launch_bounds__(256, V <= 16 ? 2 : 1) k_build_fields_rows(Fiel
           pend = v;
         ++g;
       };
-      for (uint32_t m = 0; m < p.nmat; ++m) {
-        float sx, sy, sz, pa, pui;
-        director<MORPH>(stage[m * N + x], sx, sy, sz, pa, pui);
-        const float wa = w * pa;
-        const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
-        T += f0 + f1 + f2 + f6;
-        emit(f0);
-        emit(f1);
-        emit(f2);
-        emit(wa * sx * sy);
-        emit(wa * sx * sz);
-        emit(wa * sy * sz);
-        emit(f6);
+      for (uint32_t m0 = 0; m0 < p.nmat; m0 += 4) {
+        float4 sv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (m0 + u < p.nmat) sv[u] = __ldg(&p.vox[(m0 + u) * p.nvox + i]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (m0 + u >= p.nmat) break;
+          float sx, sy, sz, pa, pui;
+          director_fields<MORPH>(sv[u], sx, sy, sz, pa, pui);
+          const float wa = w * pa;
+          const float f0 = wa * sx * sx, f1 = wa * sy * sy, f2 = wa * sz * sz, f6 = w * pui;
+          T += f0 + f1 + f2 + f6;
+          emit(f0);
+          emit(f1);
+          emit(f2);
+          emit(wa * sx * sy);
+          emit(wa * sx * sz);
+          emit(wa * sy * sz);
+          emit(f6);
+        }
       }
       emit(T);
       if (g & 1u) o[(g >> 1) * N] = make_float2(pend, 0.f);
     }
-    __syncthreads();  // lines complete; the staged voxels are no longer read
-    if (r + gridDim.x < nrows) prefetch(r + gridDim.x);  // lands while this row is transformed
+    __syncthreads();
     for (uint32_t j = warp; j < npk; j += nw) {
       float2 *line = lines + j * N;
       float2 v[V];
@@ -222,7 +218,6 @@ __global__ void __launch_bounds__(256, V <= 16 ? 2 : 1) k_build_fields_rows(Fiel
       for (int k = 0; k < V; ++k) dst[lane + 32 * k] = v[k];
     }
   }
-  cp_async_wait_all();  // no copy outlives the block
 }
 
 // Ewald projection from the packed field spectra, for a batch of energies
