@@ -298,6 +298,10 @@ struct DeviceContext {
   } f64;                                // the FP64 pipeline's buffers (plain entry points)
   Scratch main;
   DeviceBuffer vox_in, out_in;  // host-buffer entry points: morphology and projections
+  // cyr_cuda_main's compute and copy streams and its slab-upload events, made once per device and reused
+  // by every call (the calls hold `mu`)
+  cudaStream_t main_stream = nullptr, copy_stream = nullptr;
+  std::vector<cudaEvent_t> slab_events;
   // TMA column passes: the driver's tensor-map encoder, and a word set when a
   // tile copy did not complete within the kernel's wait limit
   void *encode_tiled = nullptr;
@@ -1262,6 +1266,23 @@ EwaldParams ewald_params(const Plan &pl, const cyr_options *o, const unsigned ch
 struct SlabUpload {
   uint32_t planes = 0, count = 0, issued = 0;
   std::vector<cudaEvent_t> events;
+  // events to use instead of creating them (the device context's, reused across calls): the
+  // sample event first, then one per slab; grown here when short, never destroyed here
+  std::vector<cudaEvent_t> *pool = nullptr;
+  size_t pooled = 0;
+  int next_event(cudaEvent_t *ev) {
+    if (pool) {
+      if (pooled == pool->size()) {
+        cudaEvent_t e = nullptr;
+        CYR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        pool->push_back(e);
+      }
+      *ev = (*pool)[pooled++];
+      return CYR_OK;
+    }
+    CYR_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    return CYR_OK;
+  }
   // every sample_zstep-th plane, copied first for the means (a sample spread over the volume)
   uint32_t sample_zstep = 1;
   cudaEvent_t sample = nullptr;
@@ -1290,7 +1311,7 @@ struct SlabUpload {
         a = b;
       }
       cudaEvent_t ev = nullptr;
-      CYR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      CYR_TRY(next_event(&ev));
       events.push_back(ev);
       CYR_CUDA(cudaEventRecord(ev, stream));
     }
@@ -1302,11 +1323,12 @@ struct SlabUpload {
       CYR_CUDA(cudaMemcpy2DAsync(dev + size_t(m) * nvox, pitch, host + 4 * size_t(m) * nvox, pitch,
                                  npix * sizeof(float4), (nz + sample_zstep - 1) / sample_zstep,
                                  cudaMemcpyHostToDevice, stream));
-    CYR_CUDA(cudaEventCreateWithFlags(&sample, cudaEventDisableTiming));
+    CYR_TRY(next_event(&sample));
     CYR_CUDA(cudaEventRecord(sample, stream));
     return CYR_OK;
   }
   ~SlabUpload() {
+    if (pool) return;
     for (cudaEvent_t e : events) cudaEventDestroy(e);
     if (sample) cudaEventDestroy(sample);
   }
@@ -1587,6 +1609,7 @@ struct RunMode {
   // soon as it lands, so the upload hides most of the transform
   const float *host_vox = nullptr;
   cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> *event_pool = nullptr;  // reused slab events, or null: made per call
 };
 
 
@@ -1626,6 +1649,7 @@ int run_request(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const flo
   // host morphology: uploaded in z slabs (FIELDS) or at once (per-energy spectra)
   SlabUpload upload;
   if (mode.host_vox) {
+    upload.pool = mode.event_pool;
     upload.stream = mode.copy_stream ? mode.copy_stream : st;
     if (upload.stream != st) CYR_CUDA(cudaStreamWaitEvent(upload.stream, sc.last_use, 0));
     upload.host = mode.host_vox;
@@ -2876,18 +2900,16 @@ static int cuda_main_impl(const cyr_options *opt, const float *optical, const fl
   const size_t out_bytes = size_t(o.num_energies) * nk * o.nx * o.ny * sizeof(float);
   CYR_TRY(ctx->vox_in.ensure(vox_bytes));
   CYR_TRY(ctx->out_in.ensure(out_bytes));
-  cudaStream_t st = nullptr, cs = nullptr;
-  CYR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
-    cudaStreamDestroy(st);
-    return fail(CYR_ERR_CUDA, "stream creation failed");
-  }
+  if (!ctx->main_stream) CYR_CUDA(cudaStreamCreateWithFlags(&ctx->main_stream, cudaStreamNonBlocking));
+  if (!ctx->copy_stream) CYR_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  cudaStream_t st = ctx->main_stream, cs = ctx->copy_stream;
   int rc = CYR_OK;
   do {
     // the morphology is uploaded by run_request, overlapped with the field transform (FIELDS)
     RunMode mode;
     mode.host_vox = voxels;
     mode.copy_stream = cs;
+    mode.event_pool = &ctx->slab_events;
     rc = run_request(*ctx, ctx->main, &o, optical, ctx->vox_in.as<float4>(), ctx->out_in.as<float>(), st, mode);
     if (rc != CYR_OK) break;
     if (cudaMemcpyAsync(projection, ctx->out_in.ptr, out_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
@@ -2907,8 +2929,7 @@ static int cuda_main_impl(const cyr_options *opt, const float *optical, const fl
       rc = fail(CYR_ERR_CUDA, "an FFT tile copy did not complete within its wait limit");
   } while (false);
   cudaStreamSynchronize(cs);
-  cudaStreamDestroy(cs);
-  cudaStreamDestroy(st);
+  cudaStreamSynchronize(st);
   return rc;
 }
 

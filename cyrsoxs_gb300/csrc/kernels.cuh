@@ -68,42 +68,6 @@ struct BuildParams {
 };
 
 // Direction and fractions of one material at one voxel.
-// sin and cos of an Euler angle for the FIELDS build: the angle is brought to
-// [-pi, pi] with 2 pi split into two floats (Cody-Waite), then the hardware
-// approximation is used (absolute error below 1e-6 there); angles beyond
-// +-25 rad keep the accurate library routine.  On the 256 x 512 x 512
-// request this is 0.17 ms of the fused build's 3.7 ms.
-__device__ __forceinline__ void sincos_reduced(float x, float *sn, float *cs) {
-  if (fabsf(x) <= 25.f) {
-    const float k = rintf(x * 0.159154943091895336f);  // x / (2 pi)
-    float r = fmaf(-k, 6.28318548202514648f, x);      // 2 pi rounded to float
-    r = fmaf(-k, -1.74845553146951715e-7f, r);         // minus the rounding of 2 pi
-    __sincosf(r, sn, cs);
-  } else {
-    sincosf(x, sn, cs);
-  }
-}
-
-// The director of the FIELDS build (k_build_fields, k_build_fields_rows): the
-// same as director<MORPH> with sincos_reduced for the Euler angles.
-template <int MORPH>
-__device__ __forceinline__ void director_fields(float4 s, float &sx, float &sy, float &sz, float &pa, float &pui) {
-  if (MORPH == 0) {
-    float st, ct, sp, cp;
-    sincos_reduced(s.y, &st, &ct);
-    sincos_reduced(s.z, &sp, &cp);
-    sx = cp * st;
-    sy = sp * st;
-    sz = ct;
-    pa = s.w * s.x;
-    pui = s.w - pa;
-  } else {
-    sx = s.x, sy = s.y, sz = s.z;
-    pa = 1.f;
-    pui = s.w;
-  }
-}
-
 template <int MORPH>
 __device__ __forceinline__ void director(float4 s, float &sx, float &sy, float &sz, float &pa, float &pui) {
   if (MORPH == 0) {  // Euler: s1 = (S, theta, psi, Vfrac), uniaxial.h:82-92
