@@ -2533,7 +2533,8 @@ int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerReque
     rg.nenergies = nb;
     rg.rows = p0.has_rows ? reinterpret_cast<const int2 *>(dp + off_r) + size_t(e0) * H : nullptr;
     int slot = ctx.prof.begin(kEwaldFields, st);
-    k_ewald_fields<2><<<fpix_blocks * ((nb + kEwaldEnergies - 1) / kEwaldEnergies), kFieldEwaldThreads, fsmem, st>>>(fe);
+    k_ewald_fields<2, true><<<fpix_blocks * ((nb + kEwaldEnergies - 1) / kEwaldEnergies), kFieldEwaldThreads, fsmem,
+                              st>>>(fe);
     ctx.prof.end(slot, st);
     slot = ctx.prof.begin(kRotateGram, st);
     k_rotate_gram<2, packed_energies<2>()><<<dim3(rot_tiles, (nb + nep - 1) / nep), kRotTile * kRotTile, rsm, st>>>(rg);

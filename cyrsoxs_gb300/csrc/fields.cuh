@@ -247,8 +247,8 @@ struct FieldEwaldParams {
   float4 *gram;          // NB > 0: Gram records [batch / NEP][RQ][gplane] (GramRec<NB, packed_energies<NB>()>, gram_at)
   size_t gplane;         // float4 per Gram plane (gram_plane_size(ny, nx))
   uint32_t nbatch;       // energies of this launch
-  // request group: energy e belongs to request e / e_per_req, whose packed volumes start at
-  // zspec + request * npk * nvox (DC at zdc + request * npk); 0 for a single request
+  // request group (k_ewald_fields<NB, true>): energy e belongs to request e / e_per_req, whose
+  // packed volumes start at zspec + request * npk * nvox (DC at zdc + request * npk)
   uint32_t e_per_req;
 };
 
@@ -261,7 +261,7 @@ constexpr int kFieldGather = 4;  // packed volumes whose loads are issued togeth
 // angle, per-angle images.  The energy is the fastest block index, so the
 // blocks gathering one pixel tile for neighbouring energies (nearly the same
 // Ewald sphere) run together and share the gathered sectors in L2.
-template <int NB>
+template <int NB, bool GROUP = false>
 __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldParams p) {
   // a block: 32 pixels x kEwaldEnergies neighbouring energies, one warp per
   // energy, so the warps of an SM gather nearly the same sectors (their Ewald
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   const size_t t = size_t(blockIdx.x / ngrp) * 32 + (threadIdx.x & 31);
   if (t >= npix) return;
   const uint32_t Y = uint32_t(t / nx), X = uint32_t(t % nx);
-  if (p.e_per_req) {
+  if (GROUP) {  // a request group (e_per_req > 0): this energy's request's packed volumes and DC
     const uint32_t rq = e / p.e_per_req;
     p.zspec += size_t(rq) * p.npk * p.nvox;
     p.zdc += size_t(rq) * p.npk;
