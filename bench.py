@@ -647,10 +647,11 @@ def served_benchmarks(args):
     torch.cuda.synchronize()
     spat = sum(r[5] for r in stream_reqs)
 
-    def plain_stream():
+    def plain_stream(scale=1.0):
         t0 = time.perf_counter()
         lat = []
         for arrival, o, opt, dv, dout, _ in stream_reqs:
+            arrival *= scale
             now = time.perf_counter() - t0
             if now < arrival:
                 time.sleep(arrival - now)
@@ -659,10 +660,11 @@ def served_benchmarks(args):
             lat.append(time.perf_counter() - t0 - arrival)
         return time.perf_counter() - t0, lat
 
-    def served_stream(srv):
+    def served_stream(srv, scale=1.0):
         t0 = time.perf_counter()
-        ids = []
+        ids, arrivals = [], []
         for arrival, o, opt, dv, dout, _ in stream_reqs:
+            arrival *= scale
             now = time.perf_counter() - t0
             if now < arrival:
                 time.sleep(arrival - now)
@@ -672,10 +674,20 @@ def served_benchmarks(args):
 
     plain_stream()
     tps, lps = plain_stream()
+    # the same requests at higher arrival rates (the seeded arrival times scaled): where the capacity saturates
+    sweep = []
     with serving.Server(slots=args.slots, groups=not args.no_groups) as srv:
         served_stream(srv)
         tss, lss = served_stream(srv)
         sst = srv.stats()
+        for rate in (1000.0, 5000.0):
+            scale = 200.0 / rate
+            tpr, lpr = plain_stream(scale)
+            tsr, lsr = served_stream(srv, scale)
+            sweep.append({"rate_per_s": rate, "arrival_span_s": stream_reqs[-1][0] * scale,
+                          "plain": {"patterns_per_s": spat / tpr, "seconds": tpr, **_lat_summary(lpr)},
+                          "served": {"patterns_per_s": spat / tsr, "seconds": tsr, **_lat_summary(lsr)},
+                          "speedup": tpr / tsr})
     mean_vox = sum(r[3].numel() // 4 for r in stream_reqs) / len(stream_reqs)
     out["serving"] = {
         "config": f"{len(stream_reqs)} requests, Poisson arrivals at 200/s (seeded); volume log-uniform in "
@@ -687,6 +699,7 @@ def served_benchmarks(args):
         "served": {"patterns_per_s": spat / tss, "seconds": tss, "slots": args.slots, "groups": not args.no_groups,
                    "group_runs": sst["group_runs"], "grouped_requests": sst["grouped_requests"], **_lat_summary(lss)},
         "speedup": tps / tss,
+        "rate_sweep": sweep,
     }
     del stream_reqs, shared_vox
     torch.cuda.empty_cache()
