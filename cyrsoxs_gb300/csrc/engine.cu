@@ -195,14 +195,14 @@ struct DeviceBuffer {
 enum Stage {
   kBuild = 0, kFftX, kFftY, kFftZ, kDc, kEwald, kRotate, kFill, kWarp, kMom, kMeans, kBuildZ,
   kFieldMeans, kBuildFields, kEwaldFields, kRotateGram, kFftRows, kFftColsY, kFftColsZ, kBluestein, kBuildFieldsRows,
-  kNumStages
+  kZMask, kNumStages
 };
 const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_pass<y>", "k_fft_pass<z>", "k_dc",
                                              "k_ewald_angles", "k_rotate_average", "k_fill", "k_warp",
                                              "k_moments", "k_entry_means", "k_build_fft_z",
                                              "k_field_means", "k_build_fields", "k_ewald_fields", "k_rotate_gram",
                                              "k_fft_rows", "k_fft_cols<y>", "k_fft_cols<z>", "k_bluestein",
-                                             "k_build_fields_rows"};
+                                             "k_build_fields_rows", "k_zmask"};
 
 struct Profiler {
   bool active = false;
@@ -239,6 +239,7 @@ struct ZTune {
 struct Scratch {
   DeviceBuffer spec, images, avg, params, dc, moments, means, errors, conv, flags, fmean;
   DeviceBuffer blue;               // padded lines of the Bluestein transforms
+  DeviceBuffer zmask;              // store mask of the FIELDS z pass (k_zmask)
   cudaEvent_t last_use = nullptr;  // completion of the last request that used it
   uint64_t generation = 0;         // bumped by every (re)allocation of a buffer above
   int init() {
@@ -247,29 +248,34 @@ struct Scratch {
   }
   // serving slots: stream-ordered allocations on `st`
   void bind(cudaStream_t st) {
-    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue})
+    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue, &zmask})
       b->stream = st, b->generation = &generation;
   }
   void release() {
-    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue})
+    for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue, &zmask})
       b->release();
   }
   size_t bytes() const {
     size_t n = 0;
-    for (const DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue})
+    for (const DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue, &zmask})
       n += b->bytes;
     return n;
   }
 };
 
 // Launch forms of a y or z column pass (autotuned per shape on the FIELDS path):
-// TMA tiles with a producer warp (32-column tiles for 256-point lines when nx
-// allows, 16 for 512, 8 for 1024), the block-synchronous TMA form (256-point
-// lines), or cp.async tiles.  All forms run the same warp FFT, so their
-// results are identical; kFormAuto is the fixed choice below.
-enum ColForm : uint32_t { kFormAuto = 0, kFormTmaWs = 1, kFormTmaSync = 2, kFormCp = 3 };
+// TMA tiles with a producer warp (32-column tiles in three stages for 128-
+// and 256-point lines when nx allows, 16 columns in two stages for 512, 8 for
+// 1024), the same 256-point tiles in two stages, the block-synchronous TMA
+// form (256-point lines), or cp.async tiles.  All forms run the same warp FFT,
+// so their results are identical; kFormAuto is the fixed choice below.
+enum ColForm : uint32_t { kFormAuto = 0, kFormTmaWs = 1, kFormTmaSync = 2, kFormCp = 3, kFormTmaWs2 = 4 };
 const char *form_name(uint32_t f) {
-  return f == kFormTmaWs ? "tma_ws" : f == kFormTmaSync ? "tma_sync" : f == kFormCp ? "cp_async" : "auto";
+  return f == kFormTmaWs     ? "tma_ws"
+         : f == kFormTmaWs2  ? "tma_ws2"
+         : f == kFormTmaSync ? "tma_sync"
+         : f == kFormCp      ? "cp_async"
+                             : "auto";
 }
 
 struct DeviceContext {
@@ -285,6 +291,7 @@ struct DeviceContext {
   };
   std::map<std::string, FieldTune> ftune;  // key: nx,ny,nz,npk (FIELDS path)
   bool autotune = true;                    // CYRSOXS_GB300_AUTOTUNE=0 keeps the fixed choices
+  bool zmask = true;                       // CYRSOXS_GB300_ZMASK=0: the FIELDS z pass stores every plane
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
   struct BlueTables {
@@ -326,6 +333,8 @@ int get_context(DeviceContext **out) {
     slot->device = dev;
     const char *env = std::getenv("CYRSOXS_GB300_AUTOTUNE");
     slot->autotune = !(env && std::strcmp(env, "0") == 0);
+    env = std::getenv("CYRSOXS_GB300_ZMASK");
+    slot->zmask = !(env && std::strcmp(env, "0") == 0);
   }
   *out = slot.get();
   return CYR_OK;
@@ -364,14 +373,15 @@ int setup_attrs(DeviceContext &ctx) {
 #undef CYR_WARP_Z_ATTR_V
 #undef CYR_WARP_Z_ATTR
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cols_tma_smem(256))));
-  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(cols_tma_ws_smem<1>(512))));
-  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(cols_tma_ws_smem<2>(256))));
-  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(cols_tma_ws_smem<1>(128))));
-  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(cols_tma_ws_smem<2>(128))));
+#define CYR_WS_ATTR(V, H, S)                                                                        \
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<V, H, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                int(cols_tma_ws_smem<V, H, S>())));
+  CYR_WS_ATTR(16, 1, 2)
+  CYR_WS_ATTR(8, 2, 3)
+  CYR_WS_ATTR(8, 2, 2)
+  CYR_WS_ATTR(4, 1, 2)
+  CYR_WS_ATTR(4, 2, 3)
+#undef CYR_WS_ATTR
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma64<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(cols_tma64_smem(1024))));
 #define CYR_ROWS_ATTR(M, V) \
@@ -447,9 +457,11 @@ int encode_cols_map(DeviceContext &ctx, CUtensorMap *map, void *data, uint32_t n
 }
 
 // One axis of the 3D FFT with the warp-level kernels (n = 128, 256, 512, 1024).
+// zmask: the z pass's store mask (ColTmaParams::smask), used by the forms with
+// a producer warp for 128-, 256- and 512-point lines; null stores every plane.
 template <int V>
 int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
-                    cudaStream_t st, size_t nvox, uint32_t form = kFormAuto) {
+                    cudaStream_t st, size_t nvox, uint32_t form = kFormAuto, const uint32_t *zmask = nullptr) {
   constexpr uint32_t N = 32 * V;
   const float2 *tw = nullptr;
   CYR_TRY(get_twiddles(ctx, N, &tw));
@@ -476,9 +488,15 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     k_fft_cols_tma64<32><<<grid, 9 * 32, cols_tma64_smem(N), st>>>(map, tp);
   } else if ((V == 4 || V == 8 || V == 16) && nx % kTmaCols == 0 && ctx.encode_tiled && ctx.tma_error &&
              form != kFormCp) {
-    CUtensorMap map;
+    CUtensorMap map, smap;
     CYR_TRY(encode_cols_map(ctx, &map, data, nx, ny, nz, count, nvox, axis, N < 256 ? N : 256));
+    smap = map;
     ColTmaParams tp{};
+    if (axis == 2 && zmask) {  // 8-plane boxes for the masked stores
+      CYR_TRY(encode_cols_map(ctx, &smap, data, nx, ny, nz, count, nvox, axis, 8));
+      tp.smask = zmask;
+      tp.mwords = (N / 8 + 31) / 32;
+    }
     tp.nxt = nx / kTmaCols;
     tp.others = axis == 1 ? nz : ny;
     tp.ntiles = tp.nxt * tp.others * count;
@@ -487,43 +505,46 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
     tp.error = ctx.tma_error;
     int sms = 0, per_sm = 0;
     CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
-    // 128-point lines: 32 (nx a multiple of 32) or 16 columns with a producer warp;
-    // 256-point lines: tiles of 32 columns with a producer warp (nx a multiple of
-    // 32; 256-byte runs per line), else the block-synchronous 16-column form;
-    // 512-point lines: 16 columns with a producer warp
+    // 128-point lines: 32 columns in three stages (nx a multiple of 32) or 16 in two,
+    // with a producer warp; 256-point lines: 32 columns with a producer warp in
+    // three or two stages (nx a multiple of 32; 256-byte runs per line), else the
+    // block-synchronous 16-column form; 512-point lines: 16 columns, two stages.
+    // A producer-warp form: H halves of 16 columns, S stages.
+    auto launch_ws = [&](auto vc, auto hc, auto sc) -> int {
+      constexpr int VV = decltype(vc)::value, HH = decltype(hc)::value, SS = decltype(sc)::value;
+      tp.nxt = nx / (HH * kTmaCols);
+      tp.ntiles = tp.nxt * tp.others * count;
+      constexpr size_t smem = cols_tma_ws_smem<VV, HH, SS>();
+      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<VV, HH, SS>,
+                                                             (8 * HH + 1) * 32, smem));
+      const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
+      k_fft_cols_tma_ws<VV, HH, SS><<<grid, (8 * HH + 1) * 32, smem, st>>>(map, smap, tp);
+      return CYR_OK;
+    };
+    using I4 = std::integral_constant<int, 4>;
+    using I8 = std::integral_constant<int, 8>;
+    using I16 = std::integral_constant<int, 16>;
+    using I1 = std::integral_constant<int, 1>;
+    using I2 = std::integral_constant<int, 2>;
+    using I3 = std::integral_constant<int, 3>;
     if constexpr (V == 4) {
-      auto launch_ws = [&](auto hc) -> int {
-        constexpr int HH = decltype(hc)::value;
-        tp.nxt = nx / (HH * kTmaCols);
-        tp.ntiles = tp.nxt * tp.others * count;
-        CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<4, HH>, (8 * HH + 1) * 32,
-                                                               cols_tma_ws_smem<HH>(N)));
-        const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
-        k_fft_cols_tma_ws<4, HH><<<grid, (8 * HH + 1) * 32, cols_tma_ws_smem<HH>(N), st>>>(map, tp);
-        return CYR_OK;
-      };
       if (nx % (2 * kTmaCols) == 0)
-        CYR_TRY(launch_ws(std::integral_constant<int, 2>{}));
+        CYR_TRY(launch_ws(I4{}, I2{}, I3{}));
       else
-        CYR_TRY(launch_ws(std::integral_constant<int, 1>{}));
+        CYR_TRY(launch_ws(I4{}, I1{}, I2{}));
     } else if constexpr (V == 8) {
       if (nx % (2 * kTmaCols) == 0 && form != kFormTmaSync) {
-        tp.nxt = nx / (2 * kTmaCols);
-        tp.ntiles = tp.nxt * tp.others * count;
-        CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<8, 2>, 17 * 32,
-                                                               cols_tma_ws_smem<2>(N)));
-        const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
-        k_fft_cols_tma_ws<8, 2><<<grid, 17 * 32, cols_tma_ws_smem<2>(N), st>>>(map, tp);
+        if (form == kFormTmaWs2)
+          CYR_TRY(launch_ws(I8{}, I2{}, I2{}));
+        else
+          CYR_TRY(launch_ws(I8{}, I2{}, I3{}));
       } else {
         CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma<8>, kTmaWarps * 32, cols_tma_smem(N)));
         const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
         k_fft_cols_tma<8><<<grid, kTmaWarps * 32, cols_tma_smem(N), st>>>(map, tp);
       }
     } else {
-      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<16, 1>, 9 * 32,
-                                                             cols_tma_ws_smem<1>(N)));
-      const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
-      k_fft_cols_tma_ws<16, 1><<<grid, 9 * 32, cols_tma_ws_smem<1>(N), st>>>(map, tp);
+      CYR_TRY(launch_ws(I16{}, I1{}, I2{}));
     }
   } else {
     ColPassParams cp{};
@@ -555,11 +576,11 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
 }
 
 int warp_fft_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
-                  cudaStream_t st, size_t nvox, uint32_t form = kFormAuto) {
+                  cudaStream_t st, size_t nvox, uint32_t form = kFormAuto, const uint32_t *zmask = nullptr) {
   const uint32_t n = axis == 0 ? nx : axis == 1 ? ny : nz;
-  if (n == 128) return warp_fft_pass_v<4>(ctx, data, nx, ny, nz, count, axis, st, nvox, form);
-  if (n == 256) return warp_fft_pass_v<8>(ctx, data, nx, ny, nz, count, axis, st, nvox, form);
-  if (n == 512) return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st, nvox, form);
+  if (n == 128) return warp_fft_pass_v<4>(ctx, data, nx, ny, nz, count, axis, st, nvox, form, zmask);
+  if (n == 256) return warp_fft_pass_v<8>(ctx, data, nx, ny, nz, count, axis, st, nvox, form, zmask);
+  if (n == 512) return warp_fft_pass_v<16>(ctx, data, nx, ny, nz, count, axis, st, nvox, form, zmask);
   return warp_fft_pass_v<32>(ctx, data, nx, ny, nz, count, axis, st, nvox, form);
 }
 
@@ -569,6 +590,7 @@ std::vector<uint32_t> column_forms(const DeviceContext &ctx, uint32_t n, uint32_
   const bool tma = ctx.encode_tiled && ctx.tma_error;
   if (n == 256 && tma && nx % kTmaCols == 0) {
     if (nx % (2 * kTmaCols) == 0) f.push_back(kFormTmaWs);
+    if (nx % (2 * kTmaCols) == 0) f.push_back(kFormTmaWs2);
     f.push_back(kFormTmaSync);
   }
   if ((n == 128 || n == 512) && tma && nx % kTmaCols == 0) f.push_back(kFormTmaWs);
@@ -649,7 +671,8 @@ int get_blue(DeviceContext &ctx, uint32_t n, DeviceContext::BlueTables &out) {
 }
 
 int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
-             int first, int last, size_t vstride = 0, DeviceBuffer *work = nullptr, const uint32_t *forms = nullptr);
+             int first, int last, size_t vstride = 0, DeviceBuffer *work = nullptr, const uint32_t *forms = nullptr,
+             const uint32_t *zmask = nullptr);
 
 // One axis of length n (a prime factor above 7) as a Bluestein transform, in
 // chunks of padded lines of at most 256 MB held in `work`.
@@ -717,7 +740,7 @@ int bluestein_pass(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, u
 // Lengths with a prime factor above 7 use `work` (default: the device's main
 // scratch, for callers holding the context lock).
 int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st,
-             int first, int last, size_t vstride, DeviceBuffer *work, const uint32_t *forms) {
+             int first, int last, size_t vstride, DeviceBuffer *work, const uint32_t *forms, const uint32_t *zmask) {
   const size_t nvox = vstride ? vstride : size_t(nx) * ny * nz;
   const uint32_t dims[3] = {nx, ny, nz};
   for (int axis = first; axis <= last; ++axis) {
@@ -728,7 +751,8 @@ int fft_axes(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, uint32_
       continue;
     }
     if (n == 128 || n == 256 || n == 512 || n == 1024) {
-      CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st, nvox, forms ? forms[axis] : kFormAuto));
+      CYR_TRY(warp_fft_pass(ctx, data, nx, ny, nz, count, axis, st, nvox, forms ? forms[axis] : kFormAuto,
+                            axis == 2 ? zmask : nullptr));
       continue;
     }
     if (axis > 0 && (n == 8 || n == 16 || n == 32 || n == 64) && count <= 65535) {
@@ -797,7 +821,7 @@ struct Plan {
   bool fields = false;
   uint32_t npk = 0;                     // packed field volumes
   uint32_t ebatch = 1;                  // energies per Ewald / rotation launch
-  size_t off_fcoef = 0, off_kmag = 0, off_mat = 0;
+  size_t off_fcoef = 0, off_kmag = 0, off_mat = 0, off_kvec = 0;
   uint32_t mom_zstep = 1;               // z planes between the moment samples (FIELDS)
   // LAB frame, square detector: conservative per-row column ranges of the
   // Ewald output, [k][energy][row] (ewald_rows)
@@ -1195,6 +1219,10 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
       km[e] = static_cast<float>(2 * kPi / wavelength);
     }
     pl.off_kmag = arena_put(pl.arena, km.data(), km.size());
+    std::vector<float> kv(size_t(pl.nk) * 3);
+    for (uint32_t k = 0; k < pl.nk; ++k)
+      kv[3 * k] = pl.frames[k].k.x, kv[3 * k + 1] = pl.frames[k].k.y, kv[3 * k + 2] = pl.frames[k].k.z;
+    pl.off_kvec = arena_put(pl.arena, kv.data(), kv.size());
     // per (k, angle): p_c = sum_v M[c][v] Nt_v.  LAB: p = Nt E.  MATERIAL: p = R^T Nt E.
     const uint32_t sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     std::vector<float> mat(size_t(pl.nk) * pl.nang * 18, 0.f);
@@ -1379,8 +1407,49 @@ int build_fields_x(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const 
 // launch form of the y and z passes are each timed once on the packed-field
 // buffer, before the build overwrites every element of it, and the fastest
 // kept.  Every candidate computes the same numbers.
+// Ewald geometry of a FIELDS request (k_ewald_fields); kmag, kx, ky, kz are set per energy and k.
+EwaldGeom field_geometry(const cyr_options *o, const Plan &pl) {
+  EwaldGeom g{};
+  g.start = -static_cast<float>(kPi / o->phys_size);
+  g.dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nx - 1) * 1.0));
+  g.dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.ny - 1) * 1.0));
+  g.dz = pl.twod ? 0.f : static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nz - 1) * 1.0));
+  g.nx = pl.nx, g.ny = pl.ny, g.nz = pl.nz;
+  g.interp = o->ewald_interpolation;
+  g.twod = pl.twod ? 1u : 0u;
+  return g;
+}
+
+// Store mask of the FIELDS z pass (k_zmask over the ne energies at d_kmag and
+// the nk k vectors at d_kv) in sc.zmask; *out stays null, so every plane is
+// stored, when no z-pass form of this shape takes a mask or masks are off.
+int field_zmask(DeviceContext &ctx, Scratch &sc, const EwaldGeom &g, const float *d_kmag, uint32_t ne,
+                const float *d_kv, uint32_t nk, cudaStream_t st, const uint32_t **out) {
+  *out = nullptr;
+  if (!ctx.zmask || g.twod || !(g.nz == 128 || g.nz == 256 || g.nz == 512) || g.nx % kTmaCols != 0 ||
+      !ctx.encode_tiled || !ctx.tma_error)
+    return CYR_OK;
+  const uint32_t mw = (g.nz / 8 + 31) / 32;
+  const size_t bytes = size_t(g.ny) * (g.nx / kTmaCols) * mw * sizeof(uint32_t);
+  CYR_TRY(sc.zmask.ensure(bytes));
+  CYR_CUDA(cudaMemsetAsync(sc.zmask.ptr, 0, bytes, st));
+  ZMaskParams zp{};
+  zp.g = g;
+  zp.kmag = d_kmag, zp.ne = ne;
+  zp.kv = d_kv, zp.nk = nk;
+  zp.mwords = mw;
+  zp.mask = sc.zmask.as<uint32_t>();
+  const int slot = ctx.prof.begin(kZMask, st);
+  k_zmask<<<unsigned((size_t(g.nx) * g.ny + 255) / 256), 256, 0, st>>>(zp);
+  ctx.prof.end(slot, st);
+  CYR_CUDA(cudaGetLastError());
+  *out = zp.mask;
+  return CYR_OK;
+}
+
 int tune_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan &pl, const FieldParams &fp,
-                bool fused_ok, const float2 *twx, cudaStream_t st, DeviceContext::FieldTune &ft) {
+                bool fused_ok, const float2 *twx, cudaStream_t st, DeviceContext::FieldTune &ft,
+                const uint32_t *zmask) {
   struct Cand {
     int kind;  // 0 build + x, 1 y pass, 2 z pass
     uint32_t choice;
@@ -1406,7 +1475,8 @@ int tune_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Pla
     if (c.kind == 0)
       rc = build_fields_x(ctx, sc, o, pl, fp, 0, pl.nz, c.choice == 1, twx, st);
     else
-      rc = warp_fft_pass(ctx, sc.spec.as<float2>(), pl.nx, pl.ny, pl.nz, pl.npk, c.kind, st, pl.nvox, c.choice);
+      rc = warp_fft_pass(ctx, sc.spec.as<float2>(), pl.nx, pl.ny, pl.nz, pl.npk, c.kind, st, pl.nvox, c.choice,
+                         c.kind == 2 ? zmask : nullptr);
     if (rc != CYR_OK) break;
     CYR_CUDA(cudaEventRecord(c.b, st));
   }
@@ -1458,6 +1528,11 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
     fp.hann_z = reinterpret_cast<const float *>(dp + pl.off_hz);
   }
   fp.out = spec;
+  // the planes the Ewald projection reads: the z pass stores only those
+  const EwaldGeom geom = field_geometry(o, pl);
+  const uint32_t *zmask = nullptr;
+  CYR_TRY(field_zmask(ctx, sc, geom, reinterpret_cast<const float *>(dp + pl.off_kmag), pl.ne,
+                      reinterpret_cast<const float *>(dp + pl.off_kvec), pl.nk, st, &zmask));
   // the field build fused with the x pass when x is a warp-FFT length and the row's lines fit
   const bool fused_ok = (pl.nx == 128 || pl.nx == 256 || pl.nx == 512 || pl.nx == 1024) &&
                         fields_rows_smem(pl.nx, npk, pl.nmat) <= kFftSmemBudget;
@@ -1476,7 +1551,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   if (!have) {
     ft.fused = fused_ok;
     if (ctx.autotune && !up && !capturing && !ctx.prof.active) {
-      CYR_TRY(tune_fields(ctx, sc, o, pl, fp, fused_ok, twx, st, ft));
+      CYR_TRY(tune_fields(ctx, sc, o, pl, fp, fused_ok, twx, st, ft, zmask));
       std::lock_guard<std::mutex> lk(ctx.tables_mu);
       ctx.ftune[key] = ft;
     }
@@ -1495,7 +1570,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
                      ft.form));
     if (up) CYR_TRY(const_cast<SlabUpload *>(up)->issue(sl + 1));  // the next slab's copy, behind this slab's kernels
   }
-  CYR_TRY(fft_axes(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st, 2, 2, 0, &sc.blue, ft.form));
+  CYR_TRY(fft_axes(ctx, spec, pl.nx, pl.ny, pl.nz, npk, st, 2, 2, 0, &sc.blue, ft.form, zmask));
   // bin 0 of each packed volume replaced by the mean of its neighbours
   CYR_TRY(sc.dc.ensure(size_t(kMaxPacked) * sizeof(float2)));
   int slot = ctx.prof.begin(kDc, st);
@@ -1511,13 +1586,7 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
   fe.nvox = pl.nvox;
   fe.coef = reinterpret_cast<const float4 *>(dp + pl.off_fcoef);
   fe.kmag = reinterpret_cast<const float *>(dp + pl.off_kmag);
-  fe.g.start = -static_cast<float>(kPi / o->phys_size);
-  fe.g.dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nx - 1) * 1.0));
-  fe.g.dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.ny - 1) * 1.0));
-  fe.g.dz = pl.twod ? 0.f : static_cast<float>((2.0 * kPi / o->phys_size) / ((pl.nz - 1) * 1.0));
-  fe.g.nx = pl.nx, fe.g.ny = pl.ny, fe.g.nz = pl.nz;
-  fe.g.interp = o->ewald_interpolation;
-  fe.g.twod = pl.twod ? 1u : 0u;
+  fe.g = geom;
   fe.qx = reinterpret_cast<const float *>(dp + pl.off_qx);
   fe.qy = reinterpret_cast<const float *>(dp + pl.off_qy);
   fe.qz = reinterpret_cast<const float *>(dp + pl.off_qz);
@@ -2372,6 +2441,8 @@ int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerReque
   }
   const size_t off_c = arena_put(arena, fc.data(), fc.size());
   const size_t off_k = arena_put(arena, km.data(), km.size());
+  const float kv0[3] = {p0.frames[0].k.x, p0.frames[0].k.y, p0.frames[0].k.z};
+  const size_t off_kv = arena_put(arena, kv0, 3);
   const size_t off_r = p0.has_rows ? arena_put(arena, rows.data(), rows.size()) : 0;
   const size_t off_v = arena_put(arena, vp.data(), vp.size());
   const size_t off_o = arena_put(arena, op.data(), op.size());
@@ -2476,7 +2547,12 @@ int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerReque
     CYR_CUDA(cudaGetLastError());
     CYR_TRY(fft_axes(ctx, spec, p0.nx, p0.ny, p0.nz, npk * G, st, 0, 0, 0, &sc.blue, ft.form));
   }
-  CYR_TRY(fft_axes(ctx, spec, p0.nx, p0.ny, p0.nz, npk * G, st, 1, 2, 0, &sc.blue, ft.form));
+  // the planes the Ewald projection reads for any of the G E virtual energies
+  const EwaldGeom geom = field_geometry(o, p0);
+  const uint32_t *zmask = nullptr;
+  CYR_TRY(field_zmask(ctx, sc, geom, reinterpret_cast<const float *>(dp + off_k), G * E,
+                      reinterpret_cast<const float *>(dp + off_kv), 1, st, &zmask));
+  CYR_TRY(fft_axes(ctx, spec, p0.nx, p0.ny, p0.nz, npk * G, st, 1, 2, 0, &sc.blue, ft.form, zmask));
   {
     const int slot = ctx.prof.begin(kDc, st);
     k_dc<<<1, (npk * G + 31) / 32 * 32, 0, st>>>(spec, npk * G, nvox, p0.nx, p0.ny, p0.nz, 0, 1 % p0.nz, p0.nz - 1,
@@ -2493,13 +2569,7 @@ int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerReque
   fe.coef = reinterpret_cast<const float4 *>(dp + off_c);
   fe.kmag = reinterpret_cast<const float *>(dp + off_k);
   fe.e_per_req = E;
-  fe.g.start = -static_cast<float>(kPi / o->phys_size);
-  fe.g.dx = static_cast<float>((2.0 * kPi / o->phys_size) / ((p0.nx - 1) * 1.0));
-  fe.g.dy = static_cast<float>((2.0 * kPi / o->phys_size) / ((p0.ny - 1) * 1.0));
-  fe.g.dz = p0.twod ? 0.f : static_cast<float>((2.0 * kPi / o->phys_size) / ((p0.nz - 1) * 1.0));
-  fe.g.nx = p0.nx, fe.g.ny = p0.ny, fe.g.nz = p0.nz;
-  fe.g.interp = o->ewald_interpolation;
-  fe.g.twod = p0.twod ? 1u : 0u;
+  fe.g = geom;
   fe.qx = reinterpret_cast<const float *>(dp + p0.off_qx);
   fe.qy = reinterpret_cast<const float *>(dp + p0.off_qy);
   fe.qz = reinterpret_cast<const float *>(dp + p0.off_qz);
@@ -3209,7 +3279,7 @@ int cyr_selftest_wait_limit(int *timed_out) {
       rc = fail(CYR_ERR_CUDA, "self-test setup failed");
       break;
     }
-    k_fft_cols_tma_ws<8, 2><<<1, 17 * 32, cols_tma_ws_smem<2>(ny)>>>(map, tp);
+    k_fft_cols_tma_ws<8, 2, 3><<<1, 17 * 32, cols_tma_ws_smem<8, 2, 3>()>>>(map, map, tp);
     const cudaError_t e = cudaDeviceSynchronize();
     unsigned flag = 0;
     if (e != cudaSuccess || cudaMemcpy(&flag, ctx->tma_error, sizeof flag, cudaMemcpyDeviceToHost) != cudaSuccess) {

@@ -412,4 +412,66 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   }
 }
 
+// Planes of the packed field spectra that k_ewald_fields and k_dc read, as
+// the store mask of the z pass (ColTmaParams::smask): per detector pixel, for
+// every energy and k of the request, the planes ewald_geometry gives (the
+// same float operations as k_ewald_fields, so the same planes) at the
+// pixel's column and, for the unpacking's conj Z(-k), at the mirrored column
+// and plane; plus the six neighbours of bin 0 that k_dc averages.  One bit per
+// 8 planes and 16 columns; the words are zeroed by the caller.
+constexpr uint32_t kZMaskMaxWords = 4;  // planes <= 1024
+struct ZMaskParams {
+  EwaldGeom g;          // kmag, kx, ky, kz set per energy and k
+  const float *kmag;    // [ne]
+  uint32_t ne;
+  const float *kv;      // [nk][3] k vectors (float)
+  uint32_t nk;
+  uint32_t mwords;      // words per 16-column group
+  uint32_t *mask;       // [ny][nx / 16][mwords]
+};
+
+__device__ __forceinline__ void zmask_set(const ZMaskParams &p, uint32_t x, uint32_t y, uint32_t z) {
+  const uint32_t g = z >> 3;
+  atomicOr(&p.mask[(size_t(y) * (p.g.nx >> 4) + (x >> 4)) * p.mwords + (g >> 5)], 1u << (g & 31u));
+}
+
+__global__ void __launch_bounds__(256) k_zmask(ZMaskParams p) {
+  const uint32_t nx = p.g.nx, ny = p.g.ny, nz = p.g.nz;
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t == 0) {  // the neighbours of bin 0 (dc_mean)
+    zmask_set(p, 1 % nx, 0, 0);
+    zmask_set(p, nx - 1, 0, 0);
+    zmask_set(p, 0, 1 % ny, 0);
+    zmask_set(p, 0, ny - 1, 0);
+    zmask_set(p, 0, 0, 1 % nz);
+    zmask_set(p, 0, 0, nz - 1);
+  }
+  if (t >= size_t(nx) * ny) return;
+  const uint32_t Y = uint32_t(t / nx), X = uint32_t(t % nx);
+  const uint32_t ux = igor(X, nx), uy = igor(Y, ny);
+  const uint32_t mx = ux ? nx - ux : 0u, my = uy ? ny - uy : 0u;
+  uint32_t own[kZMaskMaxWords] = {}, mir[kZMaskMaxWords] = {};
+  for (uint32_t k = 0; k < p.nk; ++k) {
+    const float kvx = p.kv[3 * k], kvy = p.kv[3 * k + 1], kvz = p.kv[3 * k + 2];
+    for (uint32_t e = 0; e < p.ne; ++e) {
+      EwaldGeom g = p.g;
+      g.kmag = p.kmag[e];
+      g.kx = __fmul_rn(g.kmag, kvx), g.ky = __fmul_rn(g.kmag, kvy), g.kz = __fmul_rn(g.kmag, kvz);
+      uint32_t zs[2];
+      float w1;
+      int nplanes;
+      if (!ewald_geometry(g, X, Y, zs[0], zs[1], w1, nplanes)) continue;
+      for (int pl = 0; pl < nplanes; ++pl) {
+        const uint32_t uz = igor(zs[pl], nz), mz = uz ? nz - uz : 0u;
+        own[(uz >> 3) >> 5] |= 1u << ((uz >> 3) & 31u);
+        mir[(mz >> 3) >> 5] |= 1u << ((mz >> 3) & 31u);
+      }
+    }
+  }
+  for (uint32_t w = 0; w < p.mwords && w < kZMaskMaxWords; ++w) {
+    if (own[w]) atomicOr(&p.mask[(size_t(uy) * (nx >> 4) + (ux >> 4)) * p.mwords + w], own[w]);
+    if (mir[w]) atomicOr(&p.mask[(size_t(my) * (nx >> 4) + (mx >> 4)) * p.mwords + w], mir[w]);
+  }
+}
+
 }  // namespace cyr

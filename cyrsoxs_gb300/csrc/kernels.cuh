@@ -903,8 +903,9 @@ __global__ void __launch_bounds__(TX * 32, cols_min_blocks(V, TX)) k_fft_cols(Co
 // exchange line.  Three forms:
 //  * k_fft_cols_tma: 8 warps, thread 0 issues the copies between tiles
 //    (256-point lines with nx a multiple of 16 but not of 32);
-//  * k_fft_cols_tma_ws<V, H>: H 16-column halves per tile, 8 H compute warps
-//    and a producer warp (512 points: H = 1; 256 points: H = 2);
+//  * k_fft_cols_tma_ws<V, H, NST>: H 16-column halves per tile, NST tile
+//    stages, 8 H compute warps and a producer warp (512 points: H = 1, two
+//    stages; 256 points: H = 2, three or two stages);
 //  * k_fft_cols_tma64: 8-column tiles with the 64-byte swizzle for
 //    1024-point lines, one column per warp.
 // (One column per warp on 16-column tiles measured slower: its 8-byte reads
@@ -924,6 +925,14 @@ struct ColTmaParams {
   // self-test of the bounded waits (cyr_selftest_wait_limit); 0 in normal use:
   uint32_t poll_limit;  // polls per wait (0: kTmaWaitPolls)
   uint32_t extra_tx;    // bytes expected beyond the tile's, so its phase never completes
+  // z pass of k_fft_cols_tma_ws only: the planes a later kernel reads, or null
+  // (every plane stored).  Bit g of word w of 16-column group (row, x / 16) at
+  // smask[(row (nx / 16) + x / 16) mwords + w] marks planes 8 (32 w + g) ..
+  // + 7 of those columns, the same in every volume.  A tile with no bit set is
+  // neither loaded nor stored; otherwise only the marked 8-plane boxes are
+  // stored (through the 8-plane store map).
+  const uint32_t *smask;
+  uint32_t mwords;
 };
 
 // Dynamic shared memory of k_fft_cols_tma: two tiles, the warps' exchange lines,
@@ -1092,34 +1101,41 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 // Warp-specialised form: H halves of 16 columns per tile (each its own
-// swizzled N x 128-byte region), 8 H compute warps (two columns each) and a
-// producer warp.  Per stage s: full[s] completes when a tile's copies have
-// landed (transaction count), empty[s] when the compute warps are done with
-// it.  The producer stores a finished tile as soon as empty[s] completes and
-// reloads the stage once that store has read it; the compute warps never wait
-// on the copies' shared-memory reads and never meet at a block barrier.
-template <int H>
-__host__ __device__ constexpr size_t cols_tma_ws_smem(uint32_t n) {
-  return 2 * size_t(H) * n * kTmaCols * 8 + size_t(8 * H) * n * 8 + size_t(n) * 8 + 32 + 1024;
+// swizzled N x 128-byte region), NST tile stages, 8 H compute warps (two
+// columns each) and a producer warp.  Per stage s: full[s] completes when a
+// tile's copies have landed (transaction count), empty[s] when the compute
+// warps are done with it.  The producer stores a finished tile as soon as
+// empty[s] completes and reloads the stage once that store has read it; the
+// compute warps never wait on the copies' shared-memory reads and never meet
+// at a block barrier.  With NST = 3 the loads run two tiles ahead of the
+// compute, which hides their latency when the stores are few (the masked z
+// pass).  Twiddles take N - R0 entries (warp_twiddles), so three stages of
+// 256-point, 32-column tiles fit the 227 KB a block may hold.
+template <int V, int H, int NST>
+__host__ __device__ constexpr size_t cols_tma_ws_smem() {
+  return size_t(NST) * H * (32 * V) * kTmaCols * 8 + size_t(8 * H) * (32 * V) * 8 +
+         size_t(32 * V - WarpPlan<V>::radix(0)) * 8 + 16 * NST + 1024;
 }
 
-template <int V, int H>
+template <int V, int H, int NST>
 __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const __grid_constant__ CUtensorMap tmap,
+                                                                          const __grid_constant__ CUtensorMap smap,
                                                                           ColTmaParams p) {
   constexpr uint32_t N = 32 * V, HALF = N * kTmaCols, TILE = H * HALF;  // float2 per half / tile
   constexpr uint32_t BOX = N < 256 ? N : 256, NBOX = N / BOX, NW = 8 * H;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  float2 *tiles = reinterpret_cast<float2 *>(base);  // [2][H][N][16], each half swizzled
-  float2 *lines = tiles + 2 * TILE;                  // [compute warps][N]
-  float2 *tws = lines + NW * N;                      // [N]
-  uint64_t *full = reinterpret_cast<uint64_t *>(tws + N), *empty = full + 2;
+  float2 *tiles = reinterpret_cast<float2 *>(base);  // [NST][H][N][16], each half swizzled
+  float2 *lines = tiles + NST * TILE;                // [compute warps][N]
+  float2 *tws = lines + NW * N;                      // [N - R0]
+  uint64_t *full = reinterpret_cast<uint64_t *>(tws + (N - WarpPlan<V>::radix(0))), *empty = full + NST;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
-    mbar_init(&empty[0], NW);
-    mbar_init(&empty[1], NW);
+#pragma unroll
+    for (int st = 0; st < NST; ++st) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], NW);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   warp_twiddles<V>(tws, p.tw);
@@ -1135,34 +1151,76 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
       c[1] = int(rest % p.others), c[2] = int(b * BOX);
     }
   };
-  auto region = [&](int s, uint32_t h, uint32_t b) { return tiles + s * TILE + h * HALF + b * BOX * kTmaCols; };
+  auto region = [&](uint32_t s, uint32_t h, uint32_t b) { return tiles + s * TILE + h * HALF + b * BOX * kTmaCols; };
+  // first mask word of half h of tile t (z pass with a store mask)
+  auto mask_at = [&](uint32_t t, uint32_t h) {
+    const uint32_t row = (t / p.nxt) % p.others;
+    return p.smask + (size_t(row) * p.nxt * H + (t % p.nxt) * H + h) * p.mwords;
+  };
+  // a tile none of whose planes is read later: the producer and the compute
+  // warps take the same decision from the same words, so their stage and
+  // phase counts stay in step
+  auto skipped = [&](uint32_t t) {
+    if (!p.smask) return false;
+    uint32_t any = 0;
+#pragma unroll
+    for (uint32_t h = 0; h < H; ++h) {
+      const uint32_t *m = mask_at(t, h);
+      for (uint32_t w = 0; w < p.mwords; ++w) any |= __ldg(&m[w]);
+    }
+    return any == 0u;
+  };
   if (warp == NW) {  // producer
     if (lane != 0) return;
-    auto store = [&](uint32_t t, int s) {
+    auto store = [&](uint32_t t, uint32_t s) {
+      if (!p.smask) {
 #pragma unroll
-      for (uint32_t h = 0; h < H; ++h)
+        for (uint32_t h = 0; h < H; ++h)
 #pragma unroll
-        for (uint32_t b = 0; b < NBOX; ++b) {
+          for (uint32_t b = 0; b < NBOX; ++b) {
+            int c[4];
+            coords(t, h, b, c);
+            tma_store_4d(&tmap, c[0], c[1], c[2], c[3], region(s, h, b));
+          }
+      } else {
+        // the marked 8-plane boxes only: box g starts 8 g lines (g KB, a
+        // multiple of the swizzle's 1024-byte period) into the half
+#pragma unroll
+        for (uint32_t h = 0; h < H; ++h) {
           int c[4];
-          coords(t, h, b, c);
-          tma_store_4d(&tmap, c[0], c[1], c[2], c[3], region(s, h, b));
+          coords(t, h, 0, c);
+          const uint32_t *m = mask_at(t, h);
+          for (uint32_t w = 0; w < p.mwords; ++w) {
+            uint32_t bits = __ldg(&m[w]);
+            while (bits) {
+              const uint32_t g = 32u * w + uint32_t(__ffs(int(bits)) - 1);
+              bits &= bits - 1u;
+              tma_store_4d(&smap, c[0], c[1], int(8 * g), c[3], region(s, h, 0) + g * 8 * kTmaCols);
+            }
+          }
         }
+      }
       bulk_commit();
     };
     bool ok = true;
-    uint32_t k = 0;
+    uint32_t k = 0;  // tiles taken by this block so far; tile k sits in stage k % NST
     const uint32_t limit = p.poll_limit ? p.poll_limit : kTmaWaitPolls;
-    int last[2] = {-1, -1};  // last tile index loaded into each stage
-    for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x, ++k) {
-      const int s = int(k & 1u);
-      if (k >= 2) {  // tile k-2 occupies stage s: store it, let the store read it, then reload
-        ok = mbar_wait(&empty[s], ((k >> 1) - 1) & 1u, limit);
+    int last[NST];         // last tile count loaded into each stage, -1: none
+    uint32_t held[NST];    // the tile each stage holds
+#pragma unroll
+    for (int st = 0; st < NST; ++st) last[st] = -1, held[st] = 0;
+    for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
+      if (skipped(t)) continue;
+      const uint32_t s = k % NST;
+      if (k >= NST) {  // the tile taken NST before occupies stage s: store it, let the store read it, then reload
+        ok = mbar_wait(&empty[s], (k / NST - 1) & 1u, limit);
         if (!ok) break;
-        store(t - 2 * gridDim.x, s);
+        store(held[s], s);
         bulk_wait_read_all();
       }
       mbar_expect_tx(&full[s], TILE * 8 + p.extra_tx);
       last[s] = int(k);
+      held[s] = t;
 #pragma unroll
       for (uint32_t h = 0; h < H; ++h)
 #pragma unroll
@@ -1171,19 +1229,19 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
           coords(t, h, b, c);
           tma_load_4d(region(s, h, b), &tmap, c[0], c[1], c[2], c[3], &full[s]);
         }
+      ++k;
     }
-    // the last (up to) two tiles
-    const uint32_t ntile = p.ntiles > blockIdx.x ? (p.ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
-    for (uint32_t kk = ntile >= 2 ? ntile - 2 : 0u; ok && kk < ntile; ++kk) {
-      const int s = int(kk & 1u);
-      ok = mbar_wait(&empty[s], (kk >> 1) & 1u, limit);
-      if (ok) store(blockIdx.x + kk * gridDim.x, s);
+    // the last (up to) NST tiles
+    for (uint32_t kk = k >= NST ? k - NST : 0u; ok && kk < k; ++kk) {
+      const uint32_t s = kk % NST;
+      ok = mbar_wait(&empty[s], (kk / NST) & 1u, limit);
+      if (ok) store(held[s], s);
     }
     if (!ok) {
       atomicOr(p.error, 1u);
       // the block must not release its shared memory under copies still landing
-      for (int st = 0; st < 2; ++st)
-        if (last[st] >= 0) mbar_drain(&full[st], (uint32_t(last[st]) >> 1) & 1u, limit, p.extra_tx, p.error);
+      for (int st = 0; st < NST; ++st)
+        if (last[st] >= 0) mbar_drain(&full[st], (uint32_t(last[st]) / NST) & 1u, limit, p.extra_tx, p.error);
     }
     bulk_wait_all();
     return;
@@ -1193,9 +1251,10 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
   const uint32_t cw = warp & 7u, hw = warp >> 3;
   const uint32_t limit = p.poll_limit ? p.poll_limit : kTmaWaitPolls;
   uint32_t k = 0;
-  for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++k) {
-    const int s = int(k & 1u);
-    if (!mbar_wait(&full[s], (k >> 1) & 1u, limit)) {
+  for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+    if (skipped(t)) continue;
+    const uint32_t s = k % NST;
+    if (!mbar_wait(&full[s], (k / NST) & 1u, limit)) {
       if (lane == 0) atomicOr(p.error, 1u);
       return;
     }
@@ -1210,15 +1269,21 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
     }
     warp_fft<V>(a, line, tws, lane);
     warp_fft<V>(c2, line, tws, lane);
+    // with a store mask only the lines of the stored 8-plane boxes are written back
+    uint32_t keep[(V + 7) / 8];
+#pragma unroll
+    for (int w = 0; w < (V + 7) / 8; ++w) keep[w] = p.smask ? __ldg(&mask_at(t, hw)[w]) : ~0u;
 #pragma unroll
     for (int i = 0; i < V; ++i) {
       const uint32_t r = lane + 32 * i;
-      *reinterpret_cast<float4 *>(tb + r * 128 + ((cw ^ (r & 7u)) << 4)) =
-          make_float4(a[i].x, a[i].y, c2[i].x, c2[i].y);
+      if ((keep[i / 8] >> ((r >> 3) & 31u)) & 1u)
+        *reinterpret_cast<float4 *>(tb + r * 128 + ((cw ^ (r & 7u)) << 4)) =
+            make_float4(a[i].x, a[i].y, c2[i].x, c2[i].y);
     }
     fence_proxy_async();  // the generic-proxy writes become visible to the bulk store
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
+    ++k;
   }
 }
 
