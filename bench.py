@@ -165,21 +165,77 @@ def load_traffic(workload):
         return {}
 
 
-def algorithmic_bytes(kernel, w, nvol, nang, planes, batch=1, npk=0):
+_ZMASK_CACHE = {}
+
+
+def zmask_fractions(w, energies):
+    """Shares of the FIELDS z pass's tiles it loads and of its 8-plane boxes it stores.
+
+    The engine's k_zmask marks, per 16 columns and 8 planes, the spectrum planes the Ewald
+    projection reads (each detector pixel's one or two planes, at its column and at the mirrored
+    column for the unpacking, for every energy; k along z) and the DC neighbours; the z pass loads
+    only tiles (32 columns for 128- and 256-point lines when nx allows, else 16) holding a mark and
+    stores only marked boxes.  (1, 1) when the z pass takes no mask (other z lengths, nx not a
+    multiple of 16)."""
+    import numpy as np
+
+    nx, ny, nz = w.nx, w.ny, w.nz
+    if nz not in (128, 256, 512) or nx % 16:
+        return 1.0, 1.0
+    key = (nx, ny, nz, w.phys_size, tuple(float(e) for e in energies))
+    if key in _ZMASK_CACHE:
+        return _ZMASK_CACHE[key]
+    f = np.float32
+    start = f(-np.pi / w.phys_size)
+    dx, dy, dz = (f((2 * np.pi / w.phys_size) / (n - 1)) for n in (nx, ny, nz))
+    X, Y = np.meshgrid(np.arange(nx), np.arange(ny))
+    posx, posy = start + X.astype(f) * dx, start + Y.astype(f) * dy
+
+    def igor(j, n):
+        return np.where(j <= n // 2, n // 2 - j, n + n // 2 - j)
+
+    ux, uy = igor(X, nx), igor(Y, ny)
+    mx, my = np.where(ux > 0, nx - ux, 0), np.where(uy > 0, ny - uy, 0)
+    boxes = np.zeros((ny, nx // 16, nz // 8), bool)
+    for e in energies:
+        kmag = f(2 * np.pi / f(1239.84197 / e))
+        val = kmag * kmag - posx * posx - posy * posy
+        ok = (val >= 0) & (X != nx - 1) & (Y != ny - 1)
+        tz = ((-kmag + np.sqrt(np.maximum(val, f(0)))) - start) / dz
+        z0 = np.where(tz <= 0, 0, tz).astype(np.int64)
+        ok &= z0 < nz - 1
+        for z in (z0, z0 + 1):
+            uz = igor(np.minimum(z, nz - 1), nz)
+            mz = np.where(uz > 0, nz - uz, 0)
+            boxes[uy[ok], ux[ok] // 16, uz[ok] // 8] = True
+            boxes[my[ok], mx[ok] // 16, mz[ok] // 8] = True
+    for (x, y, z) in ((1 % nx, 0, 0), (nx - 1, 0, 0), (0, 1 % ny, 0), (0, ny - 1, 0), (0, 0, 1), (0, 0, nz - 1)):
+        boxes[y, x // 16, z // 8] = True
+    halves = 2 if nz in (128, 256) and nx % 32 == 0 else 1
+    tiles = boxes.any(axis=2).reshape(ny, nx // (16 * halves), halves).any(axis=2)
+    out = float(tiles.mean()), float(boxes.mean())
+    _ZMASK_CACHE[key] = out
+    return out
+
+
+def algorithmic_bytes(kernel, w, nvol, nang, planes, batch=1, npk=0, energies=None):
     """Compulsory bytes per launch (each distinct element read once, written once).
 
     planes = z planes kept after the fused build + z FFT (nz when not pruned); for the FIELDS
-    strategy nvol = packed field volumes, batch = energies per Ewald/rotation launch."""
+    strategy nvol = packed field volumes, batch = energies per Ewald/rotation launch, and the z
+    pass moves the tiles and plane boxes of zmask_fractions (over `energies`, default the
+    workload's)."""
     V, P, M = w.nvox, w.nx * w.ny, w.num_material
     if npk:
         nq = 4 * (6 if nvol == 6 else 3)  # Gram bytes per pixel and energy (packed records)
+        zload, zstore = zmask_fractions(w, w.energies if energies is None else energies)
         table = {
             "k_build_fields": (16 * M + 8 * npk) * V,
             "k_build_fields_rows": (16 * M + 8 * npk) * V,  # build fused with the x pass: one write
             "k_moments": 16 * M * P * math.ceil(w.nz / max(1, w.nz // 16)),  # every (nz / 16)-th z plane
             "k_fft_rows": 2 * 8 * npk * V,
             "k_fft_cols<y>": 2 * 8 * npk * V,
-            "k_fft_cols<z>": 2 * 8 * npk * V,
+            "k_fft_cols<z>": 8 * npk * V * (zload + zstore),
             "k_fft_pass<x>": 2 * 8 * npk * V,
             "k_fft_pass<y>": 2 * 8 * npk * V,
             "k_fft_pass<z>": 2 * 8 * npk * V,
@@ -790,7 +846,7 @@ def main():
     npk = info["packed_volumes"] if info["fields"] else 0
     eb = info["energy_batch"]
     batch = len(energies) / math.ceil(len(energies) / eb)  # mean energies per batched launch
-    ab = lambda k: algorithmic_bytes(k, w, nvol, nang, planes, batch, npk)  # noqa: E731
+    ab = lambda k: algorithmic_bytes(k, w, nvol, nang, planes, batch, npk, energies)  # noqa: E731
     # dominant kernel: the largest share of the step among kernels with an algorithmic byte count
     dom = max(((k, v) for k, v in kernels.items() if ab(k)), key=lambda kv: kv[1][1])
     dom_name, (_, dom_ms, dom_n) = dom

@@ -16,14 +16,28 @@ def test_headline_algorithmic_bytes():
     V, P = 256 * 512 * 512, 512 * 512
     ab = lambda k: bench.algorithmic_bytes(k, w, 5, 36, 256, batch=50, npk=15)  # noqa: E731
     # a column pass reads and writes every packed volume once: 16.1 GB
-    assert ab("k_fft_cols<z>") == 2 * 8 * 15 * V == 16_106_127_360
-    assert ab("k_fft_rows") == ab("k_fft_cols<y>") == ab("k_fft_cols<z>")
+    assert ab("k_fft_rows") == ab("k_fft_cols<y>") == 2 * 8 * 15 * V == 16_106_127_360
+    # the z pass loads the 32-column tiles holding a plane the Ewald projection reads and stores
+    # only those 8-plane boxes
+    zl, zs = bench.zmask_fractions(w, w.energies)
+    assert 0.7 < zl < 0.9 and 0.1 < zs < 0.25
+    assert ab("k_fft_cols<z>") == 8 * 15 * V * (zl + zs)
     # the build reads 4 float4 materials and writes 15 complex volumes
     assert ab("k_build_fields") == (16 * 4 + 8 * 15) * V
     # Ewald: Z_j(k) and Z_j(-k) at two planes per pixel and energy, 3 Gram floats out
     assert ab("k_ewald_fields") == 50 * (4 * 8 * 15 * P + 12 * P)
     assert ab("k_rotate_gram") == 50 * (12 * P + 4 * P)
     assert ab("no_such_kernel") is None
+
+
+def test_zmask_fractions_cover_the_sphere_and_the_dc_neighbours():
+    # physSize 5 nm: the Ewald disc covers the detector, so every tile holds a read plane
+    w = workloads.workload("c1")
+    w = workloads.Workload("c1_z128", 128, 256, 256, 2, w.energies, w.angles, 5.0, 0, "sphere")
+    zl, zs = bench.zmask_fractions(w, w.energies)
+    assert zl == 1.0 and 0.0 < zs < 0.5
+    # lengths without a masked z pass move everything
+    assert bench.zmask_fractions(workloads.workload("z64"), [285.0]) == (1.0, 1.0)
 
 
 def test_per_energy_bytes_count_kept_planes_only():
