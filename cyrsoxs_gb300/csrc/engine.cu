@@ -204,16 +204,25 @@ const char *const kStageNames[kNumStages] = {"k_build", "k_fft_pass<x>", "k_fft_
                                              "k_fft_rows", "k_fft_cols<y>", "k_fft_cols<z>", "k_bluestein",
                                              "k_build_fields_rows", "k_zmask"};
 
+// Launches made while a stream is being captured into a CUDA graph (the
+// serving slots' graphs) are not timed: an event recorded during capture
+// becomes a graph node and cannot be waited on.  They count as dropped.  The
+// serving worker and the caller's thread both reach the profiler, so its
+// state is guarded by its own mutex.
 struct Profiler {
-  bool active = false;
+  std::atomic<bool> active{false};
+  std::mutex mu;
   std::vector<cudaEvent_t> events;  // pairs
   std::vector<int> stage;           // stage of pair i
   std::vector<int> count;           // kernel launches inside pair i
   size_t used = 0;                  // pairs recorded
   size_t dropped = 0;
   int begin(int st, cudaStream_t s, int launches = 1) {
-    if (!active) return -1;
-    if (used >= stage.size()) {
+    if (!active.load(std::memory_order_relaxed)) return -1;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!active.load(std::memory_order_relaxed)) return -1;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (used >= stage.size() || cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
       dropped += launches;
       return -1;
     }
@@ -223,7 +232,9 @@ struct Profiler {
     return int(used++);
   }
   void end(int slot, cudaStream_t s) {
-    if (slot >= 0) cudaEventRecord(events[2 * size_t(slot) + 1], s);
+    if (slot < 0) return;
+    std::lock_guard<std::mutex> lk(mu);
+    if (size_t(slot) < used) cudaEventRecord(events[2 * size_t(slot) + 1], s);
   }
 };
 
@@ -3189,6 +3200,7 @@ int cyr_profile_begin(uint32_t max_launches) {
   CYR_TRY(get_context(&ctx));
   std::lock_guard<std::mutex> lk(ctx->mu);
   Profiler &p = ctx->prof;
+  std::lock_guard<std::mutex> plk(p.mu);
   const size_t want = std::max<uint32_t>(max_launches, 1);
   while (p.events.size() < 2 * want) {
     cudaEvent_t e;
@@ -3208,16 +3220,27 @@ int cyr_profile_end(uint32_t *launches, uint32_t *calls, double *ms, uint32_t ns
   CYR_TRY(get_context(&ctx));
   std::lock_guard<std::mutex> lk(ctx->mu);
   Profiler &p = ctx->prof;
-  p.active = false;
+  size_t used = 0;
+  {
+    std::lock_guard<std::mutex> plk(p.mu);
+    p.active = false;
+    used = p.used;
+  }
   for (uint32_t i = 0; i < nstages; ++i) {
     if (launches) launches[i] = 0;
     if (calls) calls[i] = 0;
     if (ms) ms[i] = 0.0;
   }
-  for (size_t i = 0; i < p.used; ++i) {
+  for (size_t i = 0; i < used; ++i) {
     float t = 0.f;
     CYR_CUDA(cudaEventSynchronize(p.events[2 * i + 1]));
-    CYR_CUDA(cudaEventElapsedTime(&t, p.events[2 * i], p.events[2 * i + 1]));
+    // a pair whose closing event was not recorded yet (a launch of another
+    // thread still in flight when profiling stopped) is dropped
+    if (cudaEventElapsedTime(&t, p.events[2 * i], p.events[2 * i + 1]) != cudaSuccess) {
+      cudaGetLastError();
+      p.dropped += size_t(p.count[i]);
+      continue;
+    }
     const int s = p.stage[i];
     if (s >= 0 && uint32_t(s) < nstages) {
       if (launches) launches[s] += uint32_t(p.count[i]);
@@ -3225,6 +3248,7 @@ int cyr_profile_end(uint32_t *launches, uint32_t *calls, double *ms, uint32_t ns
       if (ms) ms[s] += t;
     }
   }
+  std::lock_guard<std::mutex> plk(p.mu);
   if (dropped) *dropped = uint32_t(p.dropped);
   p.used = 0;
   return CYR_OK;

@@ -236,7 +236,9 @@ CYR_API int cyr_warp_affine_device(const float *d_src, float *d_dst, int width, 
  * number of kernel launches, the number of timed calls (a call may launch a
  * matched pair of kernels of which one returns at entry) and their summed
  * duration in milliseconds.  Calls beyond max_launches are counted in
- * *dropped and not timed.
+ * *dropped and not timed, and so are launches made while their stream is
+ * being captured into a CUDA graph (the serving engine's graphs); replays of
+ * a graph are not timed either.
  */
 CYR_API int cyr_profile_begin(uint32_t max_launches);
 CYR_API int cyr_profile_end(uint32_t *launches, uint32_t *calls, double *ms, uint32_t nstages, uint32_t *dropped);

@@ -199,3 +199,21 @@ def test_groups_and_graphs_mix_with_other_requests():
             for key, rid in ids.items():
                 srv.wait(rid)
                 same(outs[key].cpu().numpy().reshape(alone[key[0]].shape), alone[key[0]])
+
+
+def test_profiling_around_graph_capture_and_replay():
+    # launches captured into a slot's graph (and its replays) are not timed; the profile still ends cleanly
+    torch, nat, serving = _setup()
+    n, o, opt, v, c = mix_requests(nat)[1]
+    want = nat.cuda_main(o, opt, v)
+    with serving.Server(slots=1, graphs=True) as srv:
+        nat.profile_begin()
+        for _ in range(3):  # warm run, capture, replay
+            out = out_for(nat, o, c)
+            srv.wait(srv.submit(o, opt, v, out))
+            same(out, want)
+        prof, dropped = nat.profile_end()
+        st = srv.stats()
+    assert st["graph_captures"] == 1 and st["graph_replays"] == 1
+    assert dropped > 0  # the captured launches
+    assert sum(v[0] for v in prof.values()) > 0  # the warm run's launches were timed
