@@ -384,8 +384,10 @@ int setup_attrs(DeviceContext &ctx) {
 #undef CYR_WARP_Z_ATTR_V
 #undef CYR_WARP_Z_ATTR
   CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(cols_tma_smem(256))));
-#define CYR_WS_ATTR(V, H, S)                                                                        \
-  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<V, H, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+#define CYR_WS_ATTR(V, H, S)                                                                               \
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<V, H, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                int(cols_tma_ws_smem<V, H, S>())));                                         \
+  CYR_CUDA(cudaFuncSetAttribute(k_fft_cols_tma_ws<V, H, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                 int(cols_tma_ws_smem<V, H, S>())));
   CYR_WS_ATTR(16, 1, 2)
   CYR_WS_ATTR(8, 2, 3)
@@ -526,10 +528,12 @@ int warp_fft_pass_v(DeviceContext &ctx, float2 *data, uint32_t nx, uint32_t ny, 
       tp.nxt = nx / (HH * kTmaCols);
       tp.ntiles = tp.nxt * tp.others * count;
       constexpr size_t smem = cols_tma_ws_smem<VV, HH, SS>();
-      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_tma_ws<VV, HH, SS>,
-                                                             (8 * HH + 1) * 32, smem));
+      // the masked form (z pass with a store mask) is its own instantiation, so
+      // the unmasked passes keep the plain tile walk and its registers
+      auto kern = tp.smask ? k_fft_cols_tma_ws<VV, HH, SS, true> : k_fft_cols_tma_ws<VV, HH, SS, false>;
+      CYR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (8 * HH + 1) * 32, smem));
       const unsigned grid = unsigned(std::min<size_t>(tp.ntiles, size_t(std::max(1, per_sm)) * sms));
-      k_fft_cols_tma_ws<VV, HH, SS><<<grid, (8 * HH + 1) * 32, smem, st>>>(map, smap, tp);
+      kern<<<grid, (8 * HH + 1) * 32, smem, st>>>(map, smap, tp);
       return CYR_OK;
     };
     using I4 = std::integral_constant<int, 4>;

@@ -1117,7 +1117,7 @@ __host__ __device__ constexpr size_t cols_tma_ws_smem() {
          size_t(32 * V - WarpPlan<V>::radix(0)) * 8 + 16 * NST + 1024;
 }
 
-template <int V, int H, int NST>
+template <int V, int H, int NST, bool MASK = false>
 __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const __grid_constant__ CUtensorMap tmap,
                                                                           const __grid_constant__ CUtensorMap smap,
                                                                           ColTmaParams p) {
@@ -1157,23 +1157,55 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
     const uint32_t row = (t / p.nxt) % p.others;
     return p.smask + (size_t(row) * p.nxt * H + (t % p.nxt) * H + h) * p.mwords;
   };
-  // a tile none of whose planes is read later: the producer and the compute
-  // warps take the same decision from the same words, so their stage and
-  // phase counts stay in step
-  auto skipped = [&](uint32_t t) {
-    if (!p.smask) return false;
-    uint32_t any = 0;
+  // The block's tiles are walked in batches of 32 candidates: lane l of a warp
+  // reads the mask words of candidate c0 + l gridDim.x (MW words per half,
+  // p.mwords == MW whenever a mask is set), and a ballot lists the tiles with
+  // a marked plane.  A tile none of whose planes is read later is neither
+  // loaded nor stored; the producer and the compute warps take the same
+  // decision from the same words, so their stage and phase counts stay in
+  // step.  One round of loads per 32 tiles keeps the mask reads off the
+  // compute warps' per-tile path.
+  // Without a mask (MASK false: p.smask is ignored) every tile is taken, in
+  // the same order.  body(t, words) runs once per taken tile and returns false
+  // to stop the walk.
+  constexpr uint32_t MW = (V + 7) / 8;
+  auto walk = [&](auto &&body) {
+    if constexpr (!MASK) {
+      uint32_t all[H][MW];
 #pragma unroll
-    for (uint32_t h = 0; h < H; ++h) {
-      const uint32_t *m = mask_at(t, h);
-      for (uint32_t w = 0; w < p.mwords; ++w) any |= __ldg(&m[w]);
+      for (uint32_t h = 0; h < H; ++h)
+#pragma unroll
+        for (uint32_t w = 0; w < MW; ++w) all[h][w] = ~0u;
+      for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x)
+        if (!body(t, all)) return;
+      return;
     }
-    return any == 0u;
+    for (uint32_t c0 = blockIdx.x; c0 < p.ntiles; c0 += 32u * gridDim.x) {
+      const uint32_t tl = c0 + lane * gridDim.x;
+      uint32_t wl[H][MW], any = 0;
+#pragma unroll
+      for (uint32_t h = 0; h < H; ++h)
+#pragma unroll
+        for (uint32_t w = 0; w < MW; ++w) {
+          wl[h][w] = tl < p.ntiles ? __ldg(&mask_at(tl, h)[w]) : 0u;
+          any |= wl[h][w];
+        }
+      uint32_t todo = __ballot_sync(0xffffffffu, tl < p.ntiles && any != 0u);
+      while (todo) {
+        const int j = __ffs(int(todo)) - 1;
+        todo &= todo - 1u;
+        uint32_t wt[H][MW];
+#pragma unroll
+        for (uint32_t h = 0; h < H; ++h)
+#pragma unroll
+          for (uint32_t w = 0; w < MW; ++w) wt[h][w] = __shfl_sync(0xffffffffu, wl[h][w], j);
+        if (!body(c0 + uint32_t(j) * gridDim.x, wt)) return;
+      }
+    }
   };
-  if (warp == NW) {  // producer
-    if (lane != 0) return;
-    auto store = [&](uint32_t t, uint32_t s) {
-      if (!p.smask) {
+  if (warp == NW) {  // producer: lane 0 issues the copies, the warp reads the mask words
+    auto store = [&](uint32_t t, uint32_t s, const uint32_t (&wm)[H][MW]) {
+      if constexpr (!MASK) {
 #pragma unroll
         for (uint32_t h = 0; h < H; ++h)
 #pragma unroll
@@ -1189,9 +1221,9 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
         for (uint32_t h = 0; h < H; ++h) {
           int c[4];
           coords(t, h, 0, c);
-          const uint32_t *m = mask_at(t, h);
-          for (uint32_t w = 0; w < p.mwords; ++w) {
-            uint32_t bits = __ldg(&m[w]);
+#pragma unroll
+          for (uint32_t w = 0; w < MW; ++w) {
+            uint32_t bits = wm[h][w];
             while (bits) {
               const uint32_t g = 32u * w + uint32_t(__ffs(int(bits)) - 1);
               bits &= bits - 1u;
@@ -1205,37 +1237,50 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
     bool ok = true;
     uint32_t k = 0;  // tiles taken by this block so far; tile k sits in stage k % NST
     const uint32_t limit = p.poll_limit ? p.poll_limit : kTmaWaitPolls;
-    int last[NST];         // last tile count loaded into each stage, -1: none
-    uint32_t held[NST];    // the tile each stage holds
+    int last[NST];               // last tile count loaded into each stage, -1: none
+    uint32_t held[NST];          // the tile each stage holds
+    uint32_t hwords[NST][H][MW]; // and its mask words
 #pragma unroll
     for (int st = 0; st < NST; ++st) last[st] = -1, held[st] = 0;
-    for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
-      if (skipped(t)) continue;
-      const uint32_t s = k % NST;
-      if (k >= NST) {  // the tile taken NST before occupies stage s: store it, let the store read it, then reload
-        ok = mbar_wait(&empty[s], (k / NST - 1) & 1u, limit);
-        if (!ok) break;
-        store(held[s], s);
-        bulk_wait_read_all();
-      }
-      mbar_expect_tx(&full[s], TILE * 8 + p.extra_tx);
-      last[s] = int(k);
-      held[s] = t;
+    if (!MASK && lane != 0) return;  // without a mask lane 0 walks the tiles alone
+    walk([&](uint32_t t, const uint32_t (&wt)[H][MW]) {
+        if (lane == 0) {
+          const uint32_t s = k % NST;
+          if (k >= NST) {  // the tile taken NST before occupies stage s: store it, let the store read it, then reload
+            ok = mbar_wait(&empty[s], (k / NST - 1) & 1u, limit);
+            if (ok) {
+              store(held[s], s, hwords[s]);
+              bulk_wait_read_all();
+            }
+          }
+          if (ok) {
+            mbar_expect_tx(&full[s], TILE * 8 + p.extra_tx);
+            last[s] = int(k);
+            held[s] = t;
 #pragma unroll
-      for (uint32_t h = 0; h < H; ++h)
+            for (uint32_t h = 0; h < H; ++h)
 #pragma unroll
-        for (uint32_t b = 0; b < NBOX; ++b) {
-          int c[4];
-          coords(t, h, b, c);
-          tma_load_4d(region(s, h, b), &tmap, c[0], c[1], c[2], c[3], &full[s]);
+              for (uint32_t w = 0; w < MW; ++w) hwords[s][h][w] = wt[h][w];
+#pragma unroll
+            for (uint32_t h = 0; h < H; ++h)
+#pragma unroll
+              for (uint32_t b = 0; b < NBOX; ++b) {
+                int c[4];
+                coords(t, h, b, c);
+                tma_load_4d(region(s, h, b), &tmap, c[0], c[1], c[2], c[3], &full[s]);
+              }
+          }
         }
-      ++k;
-    }
+        if (MASK) ok = __shfl_sync(0xffffffffu, ok, 0) != 0;
+        ++k;
+        return ok;
+    });
+    if (lane != 0) return;
     // the last (up to) NST tiles
     for (uint32_t kk = k >= NST ? k - NST : 0u; ok && kk < k; ++kk) {
       const uint32_t s = kk % NST;
       ok = mbar_wait(&empty[s], (kk / NST) & 1u, limit);
-      if (ok) store(held[s], s);
+      if (ok) store(held[s], s, hwords[s]);
     }
     if (!ok) {
       atomicOr(p.error, 1u);
@@ -1251,40 +1296,41 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
   const uint32_t cw = warp & 7u, hw = warp >> 3;
   const uint32_t limit = p.poll_limit ? p.poll_limit : kTmaWaitPolls;
   uint32_t k = 0;
-  for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-    if (skipped(t)) continue;
-    const uint32_t s = k % NST;
-    if (!mbar_wait(&full[s], (k / NST) & 1u, limit)) {
-      if (lane == 0) atomicOr(p.error, 1u);
-      return;
-    }
-    unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE + hw * HALF);
-    float2 a[V], c2[V];
+  walk([&](uint32_t, const uint32_t (&wt)[H][MW]) {
+      // with a store mask only the lines of the stored 8-plane boxes are written back
+      uint32_t keep[MW];
 #pragma unroll
-    for (int i = 0; i < V; ++i) {
-      const uint32_t r = lane + 32 * i;
-      const float4 q = *reinterpret_cast<const float4 *>(tb + r * 128 + ((cw ^ (r & 7u)) << 4));
-      a[i] = make_float2(q.x, q.y);
-      c2[i] = make_float2(q.z, q.w);
-    }
-    warp_fft<V>(a, line, tws, lane);
-    warp_fft<V>(c2, line, tws, lane);
-    // with a store mask only the lines of the stored 8-plane boxes are written back
-    uint32_t keep[(V + 7) / 8];
+      for (uint32_t w = 0; w < MW; ++w) keep[w] = H == 1 || hw == 0 ? wt[0][w] : wt[H - 1][w];
+      const uint32_t s = k % NST;
+      // the warp leaves together (the walk's ballots and shuffles need every lane)
+      if (!__all_sync(0xffffffffu, mbar_wait(&full[s], (k / NST) & 1u, limit))) {
+        if (lane == 0) atomicOr(p.error, 1u);
+        return false;
+      }
+      unsigned char *tb = reinterpret_cast<unsigned char *>(tiles + s * TILE + hw * HALF);
+      float2 a[V], c2[V];
 #pragma unroll
-    for (int w = 0; w < (V + 7) / 8; ++w) keep[w] = p.smask ? __ldg(&mask_at(t, hw)[w]) : ~0u;
+      for (int i = 0; i < V; ++i) {
+        const uint32_t r = lane + 32 * i;
+        const float4 q = *reinterpret_cast<const float4 *>(tb + r * 128 + ((cw ^ (r & 7u)) << 4));
+        a[i] = make_float2(q.x, q.y);
+        c2[i] = make_float2(q.z, q.w);
+      }
+      warp_fft<V>(a, line, tws, lane);
+      warp_fft<V>(c2, line, tws, lane);
 #pragma unroll
-    for (int i = 0; i < V; ++i) {
-      const uint32_t r = lane + 32 * i;
-      if ((keep[i / 8] >> ((r >> 3) & 31u)) & 1u)
-        *reinterpret_cast<float4 *>(tb + r * 128 + ((cw ^ (r & 7u)) << 4)) =
-            make_float4(a[i].x, a[i].y, c2[i].x, c2[i].y);
-    }
-    fence_proxy_async();  // the generic-proxy writes become visible to the bulk store
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);
-    ++k;
-  }
+      for (int i = 0; i < V; ++i) {
+        const uint32_t r = lane + 32 * i;
+        if ((keep[i / 8] >> ((r >> 3) & 31u)) & 1u)
+          *reinterpret_cast<float4 *>(tb + r * 128 + ((cw ^ (r & 7u)) << 4)) =
+              make_float4(a[i].x, a[i].y, c2[i].x, c2[i].y);
+      }
+      fence_proxy_async();  // the generic-proxy writes become visible to the bulk store
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      ++k;
+      return true;
+  });
 }
 
 // 1024-point lines: two 16-column stages do not fit shared memory, so tiles are
