@@ -266,12 +266,6 @@ struct Scratch {
     for (DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue, &zmask})
       b->release();
   }
-  size_t bytes() const {
-    size_t n = 0;
-    for (const DeviceBuffer *b : {&spec, &images, &avg, &params, &dc, &moments, &means, &errors, &conv, &flags, &fmean, &blue, &zmask})
-      n += b->bytes;
-    return n;
-  }
 };
 
 // Launch forms of a y or z column pass (autotuned per shape on the FIELDS path):

@@ -52,7 +52,7 @@ struct Build64Params {
 
 __device__ __forceinline__ void load_s64(const Build64Params &p, uint32_t m, size_t i, double s[4]) {
   if (p.vox_fp64) {
-    const double4 v = static_cast<const double4 *>(p.vox)[size_t(m) * p.nvox + i];
+    const double4_16a v = static_cast<const double4_16a *>(p.vox)[size_t(m) * p.nvox + i];
     s[0] = v.x, s[1] = v.y, s[2] = v.z, s[3] = v.w;
   } else {
     const float4 v = static_cast<const float4 *>(p.vox)[size_t(m) * p.nvox + i];

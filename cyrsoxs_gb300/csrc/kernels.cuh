@@ -1178,28 +1178,28 @@ __global__ void __launch_bounds__((8 * H + 1) * 32, 1) k_fft_cols_tma_ws(const _
         for (uint32_t w = 0; w < MW; ++w) all[h][w] = ~0u;
       for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x)
         if (!body(t, all)) return;
-      return;
-    }
-    for (uint32_t c0 = blockIdx.x; c0 < p.ntiles; c0 += 32u * gridDim.x) {
-      const uint32_t tl = c0 + lane * gridDim.x;
-      uint32_t wl[H][MW], any = 0;
-#pragma unroll
-      for (uint32_t h = 0; h < H; ++h)
-#pragma unroll
-        for (uint32_t w = 0; w < MW; ++w) {
-          wl[h][w] = tl < p.ntiles ? __ldg(&mask_at(tl, h)[w]) : 0u;
-          any |= wl[h][w];
-        }
-      uint32_t todo = __ballot_sync(0xffffffffu, tl < p.ntiles && any != 0u);
-      while (todo) {
-        const int j = __ffs(int(todo)) - 1;
-        todo &= todo - 1u;
-        uint32_t wt[H][MW];
+    } else {
+      for (uint32_t c0 = blockIdx.x; c0 < p.ntiles; c0 += 32u * gridDim.x) {
+        const uint32_t tl = c0 + lane * gridDim.x;
+        uint32_t wl[H][MW], any = 0;
 #pragma unroll
         for (uint32_t h = 0; h < H; ++h)
 #pragma unroll
-          for (uint32_t w = 0; w < MW; ++w) wt[h][w] = __shfl_sync(0xffffffffu, wl[h][w], j);
-        if (!body(c0 + uint32_t(j) * gridDim.x, wt)) return;
+          for (uint32_t w = 0; w < MW; ++w) {
+            wl[h][w] = tl < p.ntiles ? __ldg(&mask_at(tl, h)[w]) : 0u;
+            any |= wl[h][w];
+          }
+        uint32_t todo = __ballot_sync(0xffffffffu, tl < p.ntiles && any != 0u);
+        while (todo) {
+          const int j = __ffs(int(todo)) - 1;
+          todo &= todo - 1u;
+          uint32_t wt[H][MW];
+#pragma unroll
+          for (uint32_t h = 0; h < H; ++h)
+#pragma unroll
+            for (uint32_t w = 0; w < MW; ++w) wt[h][w] = __shfl_sync(0xffffffffu, wl[h][w], j);
+          if (!body(c0 + uint32_t(j) * gridDim.x, wt)) return;
+        }
       }
     }
   };
