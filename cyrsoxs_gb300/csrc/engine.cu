@@ -296,6 +296,7 @@ struct DeviceContext {
   };
   std::map<std::string, FieldTune> ftune;  // key: nx,ny,nz,npk (FIELDS path)
   bool autotune = true;                    // CYRSOXS_GB300_AUTOTUNE=0 keeps the fixed choices
+  bool sparse_ewald = true;                // CYRSOXS_GB300_SPARSE_EWALD=0 forms every combination term
   bool zmask = true;                       // CYRSOXS_GB300_ZMASK=0: the FIELDS z pass stores every plane
   bool attrs_done = false;
   std::map<uint32_t, float2 *> twiddles;
@@ -340,6 +341,8 @@ int get_context(DeviceContext **out) {
     slot->autotune = !(env && std::strcmp(env, "0") == 0);
     env = std::getenv("CYRSOXS_GB300_ZMASK");
     slot->zmask = !(env && std::strcmp(env, "0") == 0);
+    env = std::getenv("CYRSOXS_GB300_SPARSE_EWALD");
+    slot->sparse_ewald = !(env && std::strcmp(env, "0") == 0);
   }
   *out = slot.get();
   return CYR_OK;
@@ -830,6 +833,7 @@ struct Plan {
   bool fields = false;
   uint32_t npk = 0;                     // packed field volumes
   uint32_t ebatch = 1;                  // energies per Ewald / rotation launch
+  bool ewald_sparse = false;            // the combination coefficients keep their structural zeros
   size_t off_fcoef = 0, off_kmag = 0, off_mat = 0, off_kvec = 0;
   uint32_t mom_zstep = 1;               // z planes between the moment samples (FIELDS)
   // LAB frame, square detector: conservative per-row column ranges of the
@@ -1221,6 +1225,15 @@ int make_plan(const cyr_options *o, const float *optical, Plan &pl) {
               make_float4(float(al.real()), float(al.imag()), float(be.real()), float(be.imag()));
         }
     }
+    // the Ewald kernel may skip the structural zeros (coef_used) when every one of them is exactly zero
+    pl.ewald_sparse = pl.nmat <= 4;
+    for (uint32_t e = 0; e < pl.ne && pl.ewald_sparse; ++e)
+      for (int v = 0; v < 6; ++v)
+        for (uint32_t j = 0; j < npk; ++j) {
+          const float4 q = fc[(size_t(e) * 6 + v) * npk + j];
+          if (!coef_used(pl.nmat, v, j) && (q.x != 0.f || q.y != 0.f || q.z != 0.f || q.w != 0.f))
+            pl.ewald_sparse = false;
+        }
     pl.off_fcoef = arena_put(pl.arena, fc.data(), fc.size());
     std::vector<float> km(pl.ne);
     for (uint32_t e = 0; e < pl.ne; ++e) {
@@ -1644,8 +1657,17 @@ int run_fields(DeviceContext &ctx, Scratch &sc, const cyr_options *o, const Plan
       const dim3 rgrid(rot_tiles, (nb + nep - 1) / nep);
       slot = ctx.prof.begin(kEwaldFields, st);
       const unsigned fgrid = fpix_blocks * ((nb + kEwaldEnergies - 1) / kEwaldEnergies);
+      const bool sparse = pl.ewald_sparse && ctx.sparse_ewald;
       if (pl.material_frame)
         k_ewald_fields<0><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+      else if (pl.nbasis == 2 && sparse && pl.nmat == 1)
+        k_ewald_fields<2, false, 1><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+      else if (pl.nbasis == 2 && sparse && pl.nmat == 2)
+        k_ewald_fields<2, false, 2><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+      else if (pl.nbasis == 2 && sparse && pl.nmat == 3)
+        k_ewald_fields<2, false, 3><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+      else if (pl.nbasis == 2 && sparse && pl.nmat == 4)
+        k_ewald_fields<2, false, 4><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
       else if (pl.nbasis == 2)
         k_ewald_fields<2><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
       else
@@ -2435,8 +2457,10 @@ int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerReque
   std::vector<int2> rows;
   std::vector<const float4 *> vp;
   std::vector<float *> op;
+  bool sparse = nmat <= 4 && ctx.sparse_ewald;  // every member's coefficients keep the structural zeros
   for (const auto &r : g) {
     const Plan &pl = r->plan;
+    sparse = sparse && pl.ewald_sparse;
     const float4 *c = reinterpret_cast<const float4 *>(pl.arena.data() + pl.off_fcoef);
     fc.insert(fc.end(), c, c + size_t(E) * 6 * npk);
     const float *k = reinterpret_cast<const float *>(pl.arena.data() + pl.off_kmag);
@@ -2612,8 +2636,17 @@ int run_group(Server &S, Slot &sl, const std::vector<std::shared_ptr<ServerReque
     rg.nenergies = nb;
     rg.rows = p0.has_rows ? reinterpret_cast<const int2 *>(dp + off_r) + size_t(e0) * H : nullptr;
     int slot = ctx.prof.begin(kEwaldFields, st);
-    k_ewald_fields<2, true><<<fpix_blocks * ((nb + kEwaldEnergies - 1) / kEwaldEnergies), kFieldEwaldThreads, fsmem,
-                              st>>>(fe);
+    const unsigned fgrid = fpix_blocks * ((nb + kEwaldEnergies - 1) / kEwaldEnergies);
+    if (sparse && nmat == 1)
+      k_ewald_fields<2, true, 1><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+    else if (sparse && nmat == 2)
+      k_ewald_fields<2, true, 2><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+    else if (sparse && nmat == 3)
+      k_ewald_fields<2, true, 3><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+    else if (sparse && nmat == 4)
+      k_ewald_fields<2, true, 4><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
+    else
+      k_ewald_fields<2, true><<<fgrid, kFieldEwaldThreads, fsmem, st>>>(fe);
     ctx.prof.end(slot, st);
     slot = ctx.prof.begin(kRotateGram, st);
     k_rotate_gram<2, packed_energies<2>()><<<dim3(rot_tiles, (nb + nep - 1) / nep), kRotTile * kRotTile, rsm, st>>>(rg);

@@ -252,6 +252,24 @@ struct FieldEwaldParams {
   uint32_t e_per_req;
 };
 
+// Structural zeros of the combination.  Tensor entry v (xx xy xz yy yz zz)
+// takes field g = 7 m + f only when f is u_x^2, u_y^2, u_z^2 or phi_ui (the
+// diagonal, which also takes T), u_x u_y (xy), u_x u_z (xz) or u_y u_z (yz)
+// (include/uniaxial.h:94-151 in the contrast form above); coef[e][v][j] can
+// be non-zero only when field 2j or 2j+1 enters entry v.  With 4 materials
+// 34 of the 75 (entry, volume) pairs of the LAB frame's five entries are used.
+__host__ __device__ constexpr bool field_enters(uint32_t nmat, int v, uint32_t g) {
+  return g >= num_fields(nmat)        ? false                                    // T's zero partner
+         : g + 1 == num_fields(nmat)  ? (v == 0 || v == 3 || v == 5)             // T
+         : (v == 0 || v == 3 || v == 5) ? (g % kFieldsPerMaterial <= 2 || g % kFieldsPerMaterial == 6)
+         : v == 1                     ? g % kFieldsPerMaterial == 3
+         : v == 2                     ? g % kFieldsPerMaterial == 4
+                                      : g % kFieldsPerMaterial == 5;             // v == 4
+}
+__host__ __device__ constexpr bool coef_used(uint32_t nmat, int v, uint32_t j) {
+  return field_enters(nmat, v, 2 * j) || field_enters(nmat, v, 2 * j + 1);
+}
+
 constexpr int kEwaldEnergies = 4;  // energies (warps) per block
 constexpr int kFieldEwaldThreads = 32 * kEwaldEnergies;
 constexpr int kFieldGather = 4;  // packed volumes whose loads are issued together
@@ -261,7 +279,11 @@ constexpr int kFieldGather = 4;  // packed volumes whose loads are issued togeth
 // angle, per-angle images.  The energy is the fastest block index, so the
 // blocks gathering one pixel tile for neighbouring energies (nearly the same
 // Ewald sphere) run together and share the gathered sectors in L2.
-template <int NB, bool GROUP = false>
+// MT > 0: the morphology has MT materials and its coefficients keep the
+// structural zeros (coef_used), so the volumes and entries are walked at
+// compile time and the zero terms are never formed; MT = 0: any material
+// count, every term formed.
+template <int NB, bool GROUP = false, int MT = 0>
 __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldParams p) {
   // a block: 32 pixels x kEwaldEnergies neighbouring energies, one warp per
   // energy, so the warps of an SM gather nearly the same sectors (their Ewald
@@ -277,7 +299,9 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   }
   __syncthreads();
   if (eb >= p.nbatch) return;
-  const float4 *fcoef = fcoef_all + warp * 6 * p.npk;
+  constexpr uint32_t NPKC = MT > 0 ? num_packed(uint32_t(MT)) : 0u;
+  const uint32_t npk = MT > 0 ? NPKC : p.npk;
+  const float4 *fcoef = fcoef_all + warp * 6 * npk;
   const size_t npix = size_t(nx) * ny;
   const size_t t = size_t(blockIdx.x / ngrp) * 32 + (threadIdx.x & 31);
   if (t >= npix) return;
@@ -333,7 +357,7 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
   for (int pl = 0; pl < 2; ++pl)
 #pragma unroll
     for (int v = 0; v < 6; ++v) N[pl][v] = make_float2(0.f, 0.f);
-  for (uint32_t j0 = 0; j0 < p.npk; j0 += kFieldGather) {
+  auto chunk = [&](uint32_t j0) {
     float2 za[2][kFieldGather], zb[2][kFieldGather];
 #pragma unroll
     for (int q = 0; q < kFieldGather; ++q) {
@@ -341,7 +365,7 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
 #pragma unroll
       for (int pl = 0; pl < 2; ++pl) {
         za[pl][q] = zb[pl][q] = make_float2(0.f, 0.f);
-        if (j < p.npk && (pl == 0 || two)) {
+        if (j < npk && (pl == 0 || two)) {
           if (is_dc[pl]) {
             za[pl][q] = zb[pl][q] = p.zdc[j];
           } else {
@@ -355,10 +379,11 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
 #pragma unroll
     for (int q = 0; q < kFieldGather; ++q) {
       const uint32_t j = j0 + q;
-      if (j >= p.npk) break;
+      if (j >= npk) break;
 #pragma unroll
       for (int v = 0; v < 6; ++v) {
-        const float4 c = fcoef[v * p.npk + j];
+        if (MT > 0 && !coef_used(uint32_t(MT), v, j)) continue;
+        const float4 c = fcoef[v * npk + j];
 #pragma unroll
         for (int pl = 0; pl < 2; ++pl) {
           const float2 a = za[pl][q], b = make_float2(zb[pl][q].x, -zb[pl][q].y);  // b = conj Z_j(-k)
@@ -367,6 +392,12 @@ __global__ void __launch_bounds__(kFieldEwaldThreads) k_ewald_fields(FieldEwaldP
         }
       }
     }
+  };
+  if constexpr (MT > 0) {
+#pragma unroll
+    for (uint32_t j0 = 0; j0 < NPKC; j0 += kFieldGather) chunk(j0);
+  } else {
+    for (uint32_t j0 = 0; j0 < npk; j0 += kFieldGather) chunk(j0);
   }
   float Q[2][3];
 #pragma unroll
