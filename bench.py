@@ -485,7 +485,8 @@ def reference_gpu_baseline(args):
     one untimed call; median of REF_CALLS timed calls (the shared host link shows occasional
     100 ms stalls on either side).  The first configuration runs in full, with the
     FP32 build (as shipped, --use_fast_math) for Algorithm 0 and 1 and the FP64 build for
-    Algorithm 0; the larger shapes run a 2-energy sample of their request (all E angles).
+    Algorithm 0; the larger shapes (128 x 512 x 512, 256 x 512 x 512 and 256 x 1024 x 1024) run a
+    2-energy sample of their request (all E angles).
     The engine's output is also compared with the reference FP64 build's where that ran."""
     import tempfile
 
@@ -500,7 +501,7 @@ def reference_gpu_baseline(args):
     if not os.path.exists(os.path.join(refdir, "cyrsoxs_ref_fp32")):
         return {"unavailable": "the reference build (oracle/_ref) is missing: its sources were not staged"}
     specs = [("c1", None, 0, "fp32"), ("c1", None, 1, "fp32"), ("c1_aniso", None, 0, "fp64"),
-             ("c2", 2, 0, "fp32"), ("c2", 2, 1, "fp32"), ("headline", 2, 0, "fp32")]
+             ("c2", 2, 0, "fp32"), ("c2", 2, 1, "fp32"), ("headline", 2, 0, "fp32"), ("c4", 2, 0, "fp32")]
     out, cache = [], {}
 
     def pinned(a):
