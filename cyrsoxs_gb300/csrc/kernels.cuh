@@ -165,10 +165,18 @@ __global__ void __launch_bounds__(256) k_moments(MomentParams p) {
   float acc[kMoments];
 #pragma unroll
   for (int q = 0; q < kMoments; ++q) acc[q] = 0.f;
-  const size_t stride = size_t(gridDim.x) * blockDim.x;
-  const size_t plane = size_t(p.nx) * p.ny, nsamp = plane * ((p.nz + p.zstep - 1) / p.zstep);
-  for (size_t s = size_t(blockIdx.x) * blockDim.x + threadIdx.x; s < nsamp; s += stride) {
-    const size_t i = p.zstep == 1 ? s : (s / plane) * p.zstep * plane + s % plane;
+  // samples: every pixel of the planes z = 0, zstep, 2 zstep, ...; the
+  // thread's (sampled plane, pixel) position advances by the grid stride
+  // without an index division per sample
+  const size_t plane = size_t(p.nx) * p.ny, stride = size_t(gridDim.x) * blockDim.x;
+  const uint32_t nzs = (p.nz + p.zstep - 1) / p.zstep;
+  const size_t s0 = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint32_t zi = uint32_t(s0 / plane);
+  size_t pix = s0 - size_t(zi) * plane;
+  for (; zi < nzs; pix += stride) {
+    while (pix >= plane) pix -= plane, ++zi;
+    if (zi >= nzs) break;
+    const size_t i = size_t(zi) * p.zstep * plane + pix;
     float sx, sy, sz, pa, pui;
     director<MORPH>(__ldg(&p.vox[m * p.nvox + i]), sx, sy, sz, pa, pui);
     if (MORPH == 0 && p.conv) {
@@ -178,7 +186,7 @@ __global__ void __launch_bounds__(256) k_moments(MomentParams p) {
     }
     float w = 1.f;
     if (p.hann_x) {
-      const uint32_t x = uint32_t(i % p.nx), y = uint32_t((i / p.nx) % p.ny), z = uint32_t(i / (size_t(p.nx) * p.ny));
+      const uint32_t x = uint32_t(pix) % p.nx, y = uint32_t(pix) / p.nx, z = zi * p.zstep;
       w = p.hann_x[x] * p.hann_y[y] * p.hann_z[z];
     }
     const float wa = w * pa;
