@@ -306,8 +306,13 @@ struct DeviceContext {
   };
   std::map<uint32_t, BlueTables> blue;  // per Bluestein line length
   std::map<uint32_t, double2 *> tw64;   // FP64 twiddles W_n^m per length
+  struct BlueTables64 {
+    uint32_t m = 0;
+    double2 *chirp = nullptr, *bhat = nullptr;
+  };
+  std::map<uint32_t, BlueTables64> blue64;  // the FP64 pipeline's Bluestein tables per line length
   struct Fp64Scratch {
-    DeviceBuffer spec, images, avg, params, params64, vox, out;
+    DeviceBuffer spec, images, avg, params, params64, vox, out, blue;
   } f64;                                // the FP64 pipeline's buffers (plain entry points)
   Scratch main;
   DeviceBuffer vox_in, out_in;  // host-buffer entry points: morphology and projections
@@ -2103,8 +2108,10 @@ int get_tw64(DeviceContext &ctx, uint32_t n, const double2 **tw) {
 
 constexpr size_t kFft64Smem = 192 * 1024;
 
-// In-place forward FFT of `count` double volumes (7-smooth lengths).
-int fft64(DeviceContext &ctx, double2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st) {
+// One axis of the in-place forward FFT of `count` double volumes, vstride
+// elements apart (7-smooth length).
+int fft64_axis(DeviceContext &ctx, double2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
+               cudaStream_t st, size_t vstride) {
   static std::once_flag attrs;
   cudaError_t ea = cudaSuccess;
   std::call_once(attrs, [&] {
@@ -2114,10 +2121,9 @@ int fft64(DeviceContext &ctx, double2 *data, uint32_t nx, uint32_t ny, uint32_t 
   });
   CYR_CUDA(ea);
   const uint32_t dims[3] = {nx, ny, nz};
-  const size_t vstride = size_t(nx) * ny * nz;
-  for (int axis = 0; axis < 3; ++axis) {
+  {
     const uint32_t n = dims[axis];
-    if (n == 1) continue;
+    if (n == 1) return CYR_OK;
     std::vector<uint32_t> r;
     if (!factorize(n, r)) return fail(CYR_ERR_UNSUPPORTED, "FP64 path: length %u has a prime factor above 7", n);
     Fft64Params p{};
@@ -2143,6 +2149,118 @@ int fft64(DeviceContext &ctx, double2 *data, uint32_t nx, uint32_t ny, uint32_t 
   return CYR_OK;
 }
 
+// The FP64 pipeline's Bluestein tables: the chirp and FFT_m(b) / m, formed
+// on the host as for the FP32 engine (get_blue) and kept in double.
+int get_blue64(DeviceContext &ctx, uint32_t n, DeviceContext::BlueTables64 &out) {
+  std::lock_guard<std::mutex> lk(ctx.tables_mu);
+  auto it = ctx.blue64.find(n);
+  if (it != ctx.blue64.end()) {
+    out = it->second;
+    return CYR_OK;
+  }
+  const uint32_t m = bluestein_length(n);
+  std::vector<std::complex<double>> c(n), b(m, 0.0), w(m);
+  for (uint32_t j = 0; j < n; ++j) {
+    const uint64_t q = (uint64_t(j) * j) % (2 * uint64_t(n));
+    c[j] = std::polar(1.0, -kPi * double(q) / double(n));
+  }
+  for (uint32_t j = 0; j < n; ++j) {
+    b[j] = std::conj(c[j]);
+    if (j) b[m - j] = std::conj(c[j]);
+  }
+  for (uint32_t j = 0; j < m; ++j) w[j] = std::polar(1.0, -2.0 * kPi * double(j) / double(m));
+  std::vector<double2> hc(n), hb(m);
+  for (uint32_t j = 0; j < n; ++j) hc[j] = make_double2(c[j].real(), c[j].imag());
+  for (uint32_t k = 0; k < m; ++k) {
+    std::complex<double> acc(0.0, 0.0);
+    uint64_t idx = 0;  // (j k) mod m
+    for (uint32_t j = 0; j < m; ++j, idx += k) {
+      if (idx >= m) idx %= m;
+      acc += b[j] * w[idx];
+    }
+    acc /= double(m);
+    hb[k] = make_double2(acc.real(), acc.imag());
+  }
+  DeviceContext::BlueTables64 t;
+  t.m = m;
+  CYR_CUDA(cudaMalloc(&t.chirp, sizeof(double2) * n));
+  CYR_CUDA(cudaMalloc(&t.bhat, sizeof(double2) * m));
+  CYR_CUDA(cudaMemcpy(t.chirp, hc.data(), sizeof(double2) * n, cudaMemcpyHostToDevice));
+  CYR_CUDA(cudaMemcpy(t.bhat, hb.data(), sizeof(double2) * m, cudaMemcpyHostToDevice));
+  ctx.blue64[n] = t;
+  out = t;
+  return CYR_OK;
+}
+
+// One axis of length n (a prime factor above 7) of the FP64 FFT as a
+// Bluestein transform: the FP32 engine's steps (bluestein_pass) in double,
+// the padded length-m transforms by fft64_axis, in chunks of padded lines of
+// at most 256 MB held in `work`.
+int bluestein64(DeviceContext &ctx, double2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
+                cudaStream_t st, size_t vstride, DeviceBuffer *work) {
+  const uint32_t n = axis == 0 ? nx : axis == 1 ? ny : nz;
+  DeviceContext::BlueTables64 bt;
+  CYR_TRY(get_blue64(ctx, n, bt));
+  const uint32_t lpv = axis == 0 ? ny * nz : axis == 1 ? nx * nz : nx * ny;
+  const uint64_t total = uint64_t(lpv) * count;
+  const uint64_t cap = std::max<uint64_t>(1, (size_t(256) << 20) / (size_t(bt.m) * sizeof(double2)));
+  const uint32_t chunk = uint32_t(std::min<uint64_t>(total, cap));
+  CYR_TRY(work->ensure(size_t(chunk) * bt.m * sizeof(double2)));
+  int sms = 0;
+  CYR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  BlueParamsT<double2> p{};
+  p.data = data;
+  p.work = work->as<double2>();
+  p.chirp = bt.chirp;
+  p.bhat = bt.bhat;
+  p.nx = nx, p.ny = ny, p.nz = nz;
+  p.vstride = vstride;
+  p.n = n, p.m = bt.m;
+  p.lines_per_vol = lpv;
+  for (uint64_t l0 = 0; l0 < total; l0 += chunk) {
+    p.line0 = l0;
+    p.nlines = uint32_t(std::min<uint64_t>(chunk, total - l0));
+    const size_t elems = size_t(p.nlines) * bt.m;
+    const unsigned grid = unsigned(std::min<size_t>((elems + 255) / 256, size_t(sms) * 16));
+    if (axis == 0) k_blue_gather<0, double2><<<grid, 256, 0, st>>>(p);
+    if (axis == 1) k_blue_gather<1, double2><<<grid, 256, 0, st>>>(p);
+    if (axis == 2) k_blue_gather<2, double2><<<grid, 256, 0, st>>>(p);
+    CYR_CUDA(cudaGetLastError());
+    // rows of m (x lines) or columns of m (y and z lines, stored lines fastest)
+    auto padded_fft = [&]() -> int {
+      if (axis == 0) return fft64_axis(ctx, p.work, bt.m, p.nlines, 1, 1, 0, st, elems);
+      return fft64_axis(ctx, p.work, p.nlines, bt.m, 1, 1, 1, st, elems);
+    };
+    CYR_TRY(padded_fft());
+    if (axis == 0)
+      k_blue_mul<0, double2><<<grid, 256, 0, st>>>(p);
+    else
+      k_blue_mul<1, double2><<<grid, 256, 0, st>>>(p);
+    CYR_CUDA(cudaGetLastError());
+    CYR_TRY(padded_fft());
+    if (axis == 0) k_blue_scatter<0, double2><<<grid, 256, 0, st>>>(p);
+    if (axis == 1) k_blue_scatter<1, double2><<<grid, 256, 0, st>>>(p);
+    if (axis == 2) k_blue_scatter<2, double2><<<grid, 256, 0, st>>>(p);
+    CYR_CUDA(cudaGetLastError());
+  }
+  return CYR_OK;
+}
+
+// In-place forward FFT of `count` double volumes: 7-smooth axes by fft64_axis,
+// the others as Bluestein transforms.
+int fft64(DeviceContext &ctx, double2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, cudaStream_t st) {
+  const uint32_t dims[3] = {nx, ny, nz};
+  const size_t vstride = size_t(nx) * ny * nz;
+  for (int axis = 0; axis < 3; ++axis) {
+    if (dims[axis] == 1) continue;
+    if (smooth7(dims[axis]))
+      CYR_TRY(fft64_axis(ctx, data, nx, ny, nz, count, axis, st, vstride));
+    else
+      CYR_TRY(bluestein64(ctx, data, nx, ny, nz, count, axis, st, vstride, &ctx.f64.blue));
+  }
+  return CYR_OK;
+}
+
 // The FP64 path's double tables, uploaded beside the planner's float arena:
 // refractive indices per energy, Hanning tables and the E basis coefficients.
 struct Plan64 {
@@ -2154,8 +2272,9 @@ int make_plan64(const cyr_options *o, const double *optical, bool window, Plan &
   CYR_TRY(validate(o));
   if (!optical) return fail(CYR_ERR_ARGUMENT, "optical constants pointer is null");
   for (uint32_t n : {o->nx, o->ny, o->nz})
-    if (n > 1 && !smooth7(n))
-      return fail(CYR_ERR_UNSUPPORTED, "FP64 path: dimension %u has a prime factor above 7 (7-smooth lengths only)", n);
+    if (n > 1 && !smooth7(n) && (n > (kMaxBluesteinPad + 1) / 2 || bluestein_length(n) > kMaxBluesteinPad))
+      return fail(CYR_ERR_UNSUPPORTED, "FP64 path: dimension %u has a prime factor above 7 and exceeds the Bluestein "
+                  "limit of 2048", n);
   // geometry (k frames, E rotations, q tables, warp coefficients) from the FP32 planner
   std::vector<float> of(size_t(o->num_energies) * o->num_material * 4);
   for (size_t i = 0; i < of.size(); ++i) of[i] = float(optical[i]);

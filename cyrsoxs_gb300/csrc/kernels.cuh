@@ -599,11 +599,13 @@ __global__ void __launch_bounds__(kFftThreads, 3) k_fft_pass(FftPassParams p) {
 // for y and z lines (a column pass), so every gather, product and scatter
 // reads and writes contiguous memory.
 // ---------------------------------------------------------------------------
-struct BlueParams {
-  float2 *data;           // the volumes being transformed
-  float2 *work;           // x lines: [nlines][m]; y and z lines: [m][nlines] (lines fastest)
-  const float2 *chirp;    // c_j, j < n
-  const float2 *bhat;     // FFT_m(b) / m
+// T = float2 for the FP32 engine, double2 for the FP64 pipeline (its tables in double).
+template <class T>
+struct BlueParamsT {
+  T *data;                // the volumes being transformed
+  T *work;                // x lines: [nlines][m]; y and z lines: [m][nlines] (lines fastest)
+  const T *chirp;         // c_j, j < n
+  const T *bhat;          // FFT_m(b) / m
   uint32_t nx, ny, nz;    // volume dimensions (nz: the planes this call covers)
   size_t vstride;         // elements between volumes
   uint32_t n, m;          // line length, padded length
@@ -611,10 +613,15 @@ struct BlueParams {
   uint32_t nlines;        // lines in this chunk
   uint32_t lines_per_vol; // x pass: ny nz; y pass: nx nz; z pass: nx ny
 };
+using BlueParams = BlueParamsT<float2>;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
 
 // Offset of line `line` and the stride between its elements.
-template <int AXIS>
-__device__ __forceinline__ size_t blue_line(const BlueParams &p, uint64_t line, size_t &estep) {
+template <int AXIS, class P>
+__device__ __forceinline__ size_t blue_line(const P &p, uint64_t line, size_t &estep) {
   const uint64_t v = line / p.lines_per_vol;
   const uint32_t r = uint32_t(line % p.lines_per_vol);
   size_t base = v * p.vstride;
@@ -634,8 +641,8 @@ __device__ __forceinline__ size_t blue_line(const BlueParams &p, uint64_t line, 
 // work = x_j c_j (j < n), 0 (n <= j < m).  Thread t takes element t of the
 // work buffer, so its stores are contiguous; for y and z lines consecutive
 // lines are consecutive x, so the volume reads are contiguous too.
-template <int AXIS>
-__global__ void k_blue_gather(BlueParams p) {
+template <int AXIS, class T = float2>
+__global__ void k_blue_gather(BlueParamsT<T> p) {
   const size_t total = size_t(p.nlines) * p.m;
   for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
     uint32_t l, j;
@@ -644,7 +651,7 @@ __global__ void k_blue_gather(BlueParams p) {
     } else {
       l = uint32_t(t % p.nlines), j = uint32_t(t / p.nlines);
     }
-    float2 v = make_float2(0.f, 0.f);
+    T v{};
     if (j < p.n) {
       size_t es;
       const size_t b = blue_line<AXIS>(p, p.line0 + l, es);
@@ -655,18 +662,18 @@ __global__ void k_blue_gather(BlueParams p) {
 }
 
 // work = conj(work * bhat): the product of the transforms, conjugated for the inverse
-template <int AXIS>
-__global__ void k_blue_mul(BlueParams p) {
+template <int AXIS, class T = float2>
+__global__ void k_blue_mul(BlueParamsT<T> p) {
   const size_t total = size_t(p.nlines) * p.m;
   for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
-    const float2 w = cmul(p.work[t], p.bhat[AXIS == 0 ? t % p.m : t / p.nlines]);
-    p.work[t] = make_float2(w.x, -w.y);
+    const T w = cmul(p.work[t], p.bhat[AXIS == 0 ? t % p.m : t / p.nlines]);
+    p.work[t] = T{w.x, -w.y};
   }
 }
 
 // x_k = c_k conj(work element k of line l), k < n
-template <int AXIS>
-__global__ void k_blue_scatter(BlueParams p) {
+template <int AXIS, class T = float2>
+__global__ void k_blue_scatter(BlueParamsT<T> p) {
   const size_t total = size_t(p.nlines) * p.n;
   for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
     uint32_t l, k;
@@ -678,10 +685,10 @@ __global__ void k_blue_scatter(BlueParams p) {
       l = uint32_t(t % p.nlines), k = uint32_t(t / p.nlines);
       wi = t;  // element k of line l at k nlines + l
     }
-    const float2 w = p.work[wi];
+    const T w = p.work[wi];
     size_t es;
     const size_t b = blue_line<AXIS>(p, p.line0 + l, es);
-    p.data[b + k * es] = cmul(p.chirp[k], make_float2(w.x, -w.y));
+    p.data[b + k * es] = cmul(p.chirp[k], T{w.x, -w.y});
   }
 }
 

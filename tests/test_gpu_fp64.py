@@ -5,7 +5,8 @@ cyr_compute_polarization_fp64): the drop-in for the reference's
 * Against the FP64 CPU oracle on the golden cases (the same float decisions,
   every amplitude in double): max relative error <= 1e-10 over pixels above
   1e-6 of the peak, identical NaN masks; polarization <= 1e-12 of the
-  largest component.
+  largest component.  The same bound holds on axis lengths with a prime
+  factor above 7 (Bluestein transforms in double).
 * The device-resident form on the FP32 path's own float4 voxels equals the
   host form.
 * The reference's harness built with -DDOUBLE_PRECISION runs through the shim
@@ -22,7 +23,7 @@ import pytest
 
 import cases
 import oracle
-from test_gpu_parity import native, options_for, rel_err
+from test_gpu_parity import PRIME, native, options_for, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -38,6 +39,18 @@ FP64_CASES = ["euler_sphere", "euler_hanning_mask", "vector_nn_full", "vector_li
 def test_fp64_pipeline_matches_cpu_oracle(name):
     nat = native()
     case = cases.CASES[name]
+    got = nat.cuda_main_fp64(options_for(case), cases.optical_constants(case), cases.voxels(case))
+    want = oracle.run_case(case)
+    assert np.array_equal(np.isnan(got), np.isnan(want)), "NaN mask differs from the oracle"
+    e = rel_err(got, want)
+    assert e.max() <= 1e-10, e.max()
+
+
+# lengths with a prime factor above 7: Bluestein transforms in double on the affected axes (x, y and z; the
+# z pass and the x pass of a 2D case), as the reference's FP64 build transforms them with cuFFT's Z2Z plans
+@pytest.mark.parametrize("case", PRIME, ids=[c.name for c in PRIME])
+def test_fp64_pipeline_prime_lengths_match_cpu_oracle(case):
+    nat = native()
     got = nat.cuda_main_fp64(options_for(case), cases.optical_constants(case), cases.voxels(case))
     want = oracle.run_case(case)
     assert np.array_equal(np.isnan(got), np.isnan(want)), "NaN mask differs from the oracle"
