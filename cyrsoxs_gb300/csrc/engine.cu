@@ -299,6 +299,7 @@ struct DeviceContext {
   bool sparse_ewald = true;                // CYRSOXS_GB300_SPARSE_EWALD=0 forms every combination term
   bool zmask = true;                       // CYRSOXS_GB300_ZMASK=0: the FIELDS z pass stores every plane
   bool attrs_done = false;
+  bool attrs64 = false;                    // the FP64 FFT kernels' shared-memory attribute is set
   std::map<uint32_t, float2 *> twiddles;
   struct BlueTables {
     uint32_t m = 0;
@@ -2112,14 +2113,12 @@ constexpr size_t kFft64Smem = 192 * 1024;
 // elements apart (7-smooth length).
 int fft64_axis(DeviceContext &ctx, double2 *data, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t count, int axis,
                cudaStream_t st, size_t vstride) {
-  static std::once_flag attrs;
-  cudaError_t ea = cudaSuccess;
-  std::call_once(attrs, [&] {
-    ea = cudaFuncSetAttribute(k64_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem));
-    if (ea == cudaSuccess) ea = cudaFuncSetAttribute(k64_fft<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem));
-    if (ea == cudaSuccess) ea = cudaFuncSetAttribute(k64_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem));
-  });
-  CYR_CUDA(ea);
+  if (!ctx.attrs64) {  // once per device (the attribute belongs to the current device)
+    CYR_CUDA(cudaFuncSetAttribute(k64_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem)));
+    CYR_CUDA(cudaFuncSetAttribute(k64_fft<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem)));
+    CYR_CUDA(cudaFuncSetAttribute(k64_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFft64Smem)));
+    ctx.attrs64 = true;
+  }
   const uint32_t dims[3] = {nx, ny, nz};
   {
     const uint32_t n = dims[axis];
