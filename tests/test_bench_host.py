@@ -1,7 +1,9 @@
 """Host-side pieces of the benchmark, on CPU: the algorithmic byte counts the
 roofline divides by, the latency percentiles, the median of repeated passes,
-the clock-record parser, the precision metric and the seeded workloads."""
+the clock-record parser, the precision metric, the seeded workloads and the
+reference arm's JSON line."""
 import json
+import os
 
 import numpy as np
 import pytest
@@ -131,3 +133,25 @@ def test_energy_shards_repeat_energies_beyond_the_list():
     shards = [bench.shard_energies(es, r, 2, 3) for r in range(2)]
     flat = shards[0] + shards[1]
     assert len(set(flat)) == 6 and shards[0][:2] == es
+
+
+def test_reference_arm_prints_one_contract_line():
+    # the reference arm (the FP64 port on the host cores) on the small workload: one JSON line with the
+    # contract's keys, its own cpu_baseline, and an e2e with no device copies
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    p = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "small", "--steps", "2",
+                        "--warmup", "1"], capture_output=True, text=True, timeout=300, cwd=root)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, p.stdout
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["steps"] == 2 and d["warmup"] == 1 and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
